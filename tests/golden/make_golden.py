@@ -1,0 +1,215 @@
+"""Generate golden vectors by running the Tichi_SPH reference's own kernels.
+
+Test infrastructure, run by hand in a container that holds the reference source
+(``python tests/golden/make_golden.py [scene ...]``); the fixtures it writes are
+committed and the tests never need the reference at run time.
+
+Taichi is not installed here, so the reference modules are imported on top of the
+pure-Python Taichi stand-in in ``tests/golden/taichi_shim`` and every kernel body of
+``sph.py`` / ``sph_obj.py`` / ``sph_util.py`` / ``sph_config.py`` runs as written.
+The reference's ``main.py`` cannot be imported (it opens a GGUI window at import,
+``main.py:383-415``), so ``_substep`` below replays its per-substep sequence:
+``run_step`` (``main.py:339-352``) and ``sph_step`` (``main.py:175-256``), with the
+volume-fraction (FBM) block ``main.py:244-250`` enabled for VFSPH scenes.
+
+For each scene in ``tests/golden/scenes`` two child processes run:
+
+1. ``TAICHI_SHIM_FP=f32``: the reference's emitters (``scene_add_cube`` /
+   ``scene_add_box``, ``sph_obj.py:102-180``) build the initial state with f32
+   field stores, exactly as Taichi's ``default_fp=f32`` would; VFSPH scenes then get
+   seeded per-particle volume-fraction noise and the reference's ``SPH_update_mass``.
+   Saved as ``<scene>.init.npz``.
+2. ``TAICHI_SHIM_FP=f64``: the same objects, loaded with that initial state, are
+   stepped ``STEPS[scene]`` substeps with f64 field storage; every field and
+   counter after each substep is saved as ``<scene>.steps.npz``.  f64 storage makes
+   these the reference algorithm's values without f32 rounding, which is what the
+   FP64 oracle is pinned against.
+"""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("TICHI_REFERENCE", "/root/reference")
+SCENES = os.path.join(HERE, "scenes")
+STEPS = {"dfsph2d": 3, "dfsph2d_r2": 2, "dfsph3d": 2, "vfsph2d": 3, "vfsph3d": 2, "edge2d": 2}
+FBM_SCENES = {"vfsph2d", "vfsph3d"}
+VF_NOISE_SEED = 3
+
+PARTICLE_FIELDS = [
+    "pos", "vel", "vel_adv", "acce", "acce_adv", "mass", "rest_density", "rest_volume",
+    "volume_frac", "volume_frac_tmp", "W", "sph_density", "sph_compression", "psi_adv",
+    "alpha", "alpha_1", "alpha_2", "normal", "drift_vel", "fbm_zeta", "flag",
+    "neighb_cell_seq", "neighb_cell_structured_seq", "pressure", "pressure_force", "W_grad",
+]
+STATE_IN = ["pos", "vel", "volume_frac", "rest_volume", "mass", "rest_density"]
+
+
+def _child(scene, mode):
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, os.path.join(HERE, "taichi_shim"))
+    sys.path.insert(0, REF)
+    sys.argv = ["main.py", "-c", os.path.join(SCENES, scene + ".config.json"),
+                "-s", os.path.join(SCENES, scene + ".scenario.json")]
+    import sph  # noqa: E402  (runs sph_config at import, sph_config.py:27-235)
+    R = sph
+    config = R.config
+    # main.py:8-12 without the Eulerian Grid (unused; it would allocate 328^3 cells)
+    ngrid = R.Ngrid()
+    fluid = R.Fluid(max_part_num=config.fluid_max_part_num[None])
+    bound = R.Fluid(max_part_num=config.bound_max_part_num[None])
+    objs = {"fluid": fluid, "bound": bound}
+    # init_scenario / add_to_scenario, main.py:42-79 (cube and box only)
+    for part in R.scenario_buffer:
+        if part == "sim_env":
+            continue
+        for param in R.scenario_buffer[part]["objs"]:
+            obj = objs[part]
+            if param["type"] == "cube":
+                obj.scene_add_cube(param["start_pos"], param["end_pos"], param["volume_frac"],
+                                   param["vel"], int(param["color"], 16), param["particle_relaxing_factor"])
+            elif param["type"] == "box":
+                obj.scene_add_box(param["start_pos"], param["end_pos"], param["layers"],
+                                  param["volume_frac"], param["vel"], int(param["color"], 16),
+                                  param["particle_relaxing_factor"])
+            else:
+                raise RuntimeError("golden scenes use cube/box objects only")
+
+    if mode == "f32":
+        if scene in FBM_SCENES:
+            # seeded +-0.05 noise on the volume fractions, clipped and renormalised
+            rng = np.random.default_rng(VF_NOISE_SEED)
+            n = fluid.part_num[None]
+            vf = fluid.volume_frac.to_numpy()
+            noisy = np.clip(vf[:n] + rng.uniform(-0.05, 0.05, vf[:n].shape), 0.0, 1.0)
+            noisy /= noisy.sum(axis=1, keepdims=True)
+            vf[:n] = noisy.astype(np.float32)
+            fluid.volume_frac.from_numpy(vf)
+            R.SPH_update_mass(fluid)
+        out = {"solver_type": R.solver_type}
+        for name, obj in objs.items():
+            n = obj.part_num[None]
+            out[name + "_n"] = n
+            for f in STATE_IN:
+                out[name + "_" + f] = getattr(obj, f).to_numpy()[:n]
+        np.savez_compressed(os.path.join(HERE, scene + ".init.npz"), **out)
+        return
+
+    init = np.load(os.path.join(HERE, scene + ".init.npz"))
+    for name, obj in objs.items():
+        n = int(init[name + "_n"])
+        assert obj.part_num[None] == n, (name, obj.part_num[None], n)
+        for f in STATE_IN:
+            arr = getattr(obj, f).to_numpy()
+            arr[:n] = init[name + "_" + f]
+            getattr(obj, f).from_numpy(arr)
+
+    gv = R.GlobalVariable()
+    fbm = scene in FBM_SCENES
+    rec = {}
+    for step in range(STEPS[scene]):
+        _substep(R, config, ngrid, fluid, bound, gv, fbm)
+        p = "s%d_" % step
+        rec[p + "dt"] = config.dt[None]
+        rec[p + "time_count"] = gv.time_count
+        rec[p + "div_iter"] = gv.div_iter_count
+        rec[p + "incom_iter"] = gv.incom_iter_count
+        rec[p + "compression"] = fluid.compression[None]
+        rec[p + "kinetic_energy"] = fluid.statistics_kinetic_energy[None]
+        rec[p + "potential_energy"] = fluid.statistics_gravity_potential_energy[None]
+        rec[p + "general_flag"] = fluid.general_flag[None]
+        for name, obj in objs.items():
+            n = obj.part_num[None]
+            for f in PARTICLE_FIELDS:
+                rec[p + name + "_" + f] = getattr(obj, f).to_numpy()[:n]
+        print("  %s step %d: dt=%.6g div=%d incom=%d compression=%.6g" % (
+            scene, step, config.dt[None], gv.div_iter_count, gv.incom_iter_count,
+            fluid.compression[None]), flush=True)
+    np.savez_compressed(os.path.join(HERE, scene + ".steps.npz"), **rec)
+
+
+def _substep(R, config, ngrid, fluid, bound, gv, fbm):
+    """run_step's substep body (main.py:347-352) around sph_step (main.py:175-256)."""
+    R.cfl_condition(fluid)
+    gv.time_count += config.dt[None]
+    # sph_step
+    ngrid.clear_node()
+    ngrid.encode(fluid)
+    ngrid.encode(bound)
+    ngrid.mem_shift()
+    ngrid.fill_node(fluid)
+    ngrid.fill_node(bound)
+    R.SPH_clean_value(fluid)
+    R.SPH_clean_value(bound)
+    R.SPH_prepare_attr(ngrid, fluid, fluid)
+    R.SPH_prepare_attr(ngrid, fluid, bound)
+    R.SPH_prepare_attr(ngrid, bound, bound)
+    R.SPH_prepare_attr(ngrid, bound, fluid)
+    R.SPH_prepare_alpha_1(ngrid, fluid, fluid)
+    R.SPH_prepare_alpha_1(ngrid, fluid, bound)
+    R.SPH_prepare_alpha_2(ngrid, fluid, fluid)
+    R.SPH_prepare_alpha_2(ngrid, bound, fluid)
+    R.SPH_prepare_alpha(fluid)
+    R.SPH_prepare_alpha(bound)
+    gv.div_iter_count = 0
+    R.SPH_vel_2_vel_adv(fluid)
+    while gv.div_iter_count < config.iter_threshold_min[None] or \
+            fluid.compression[None] > config.divergence_threshold[None]:
+        R.IPPE_adv_psi_init(fluid)
+        R.IPPE_adv_psi(ngrid, fluid, fluid)
+        R.IPPE_adv_psi(ngrid, fluid, bound)
+        R.IPPE_psi_adv_non_negative(fluid)
+        R.IPPE_update_vel_adv(ngrid, fluid, fluid)
+        R.IPPE_update_vel_adv(ngrid, fluid, bound)
+        gv.div_iter_count += 1
+        if gv.div_iter_count > config.iter_threshold_max[None]:
+            break
+    R.SPH_vel_adv_2_vel(fluid)
+    R.SPH_advection_gravity_acc(fluid)
+    R.SPH_advection_viscosity_acc(ngrid, fluid, fluid)
+    R.SPH_advection_surface_tension_acc(ngrid, fluid, fluid)
+    R.SPH_advection_update_vel_adv(fluid)
+    gv.incom_iter_count = 0
+    while gv.incom_iter_count < config.iter_threshold_min[None] or \
+            fluid.compression[None] > config.compression_threshold[None]:
+        R.IPPE_adv_psi_init(fluid)
+        R.IPPE_adv_psi(ngrid, fluid, fluid)
+        R.IPPE_adv_psi(ngrid, fluid, bound)
+        R.IPPE_psi_adv_non_negative(fluid)
+        R.IPPE_update_vel_adv(ngrid, fluid, fluid)
+        R.IPPE_update_vel_adv(ngrid, fluid, bound)
+        gv.incom_iter_count += 1
+        if gv.incom_iter_count > config.iter_threshold_max[None]:
+            break
+    if fbm:  # main.py:244-250, enabled
+        while fluid.general_flag[None] > 0:
+            R.SPH_FBM_clean_tmp(fluid)
+            R.SPH_FBM_convect(ngrid, fluid, fluid)
+            R.SPH_FBM_diffuse(ngrid, fluid, fluid)
+            R.SPH_FBM_check_tmp(fluid)
+        R.SPH_update_volume_frac(fluid)
+    R.SPH_update_mass(fluid)
+    R.SPH_update_pos(fluid)
+    R.SPH_update_energy(fluid)
+    gv.frame_div_iter += gv.div_iter_count
+    gv.frame_incom_iter += gv.incom_iter_count
+
+
+def main(argv):
+    if len(argv) >= 3 and argv[0] == "--child":
+        _child(argv[1], argv[2])
+        return
+    scenes = argv or sorted(STEPS)
+    for scene in scenes:
+        for mode in ("f32", "f64"):
+            print("scene %s (%s)" % (scene, mode), flush=True)
+            env = dict(os.environ, TAICHI_SHIM_FP=mode)
+            subprocess.run([sys.executable, os.path.abspath(__file__), "--child", scene, mode],
+                           env=env, check=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
