@@ -1,0 +1,162 @@
+/*
+ * tichi_sph.h -- C ABI of the GB300 (sm_103a) SPH hot path.
+ *
+ * Drop-in boundary for the per-substep solver of Tichi_SPH.  Every entry point
+ * takes plain C types: device pointers to particle arrays that the caller owns
+ * (the host side keeps them as PyTorch CUDA tensors), sizes, and a CUDA stream
+ * passed as `void *` (a `cudaStream_t`; NULL = legacy default stream).  No entry
+ * point allocates memory except tsph_create.  All calls are stream-ordered; only
+ * tsph_read_stats and tsph_neighbor_stats synchronise the stream.
+ *
+ * Each declaration names the reference interface it replaces (paths are within
+ * the Tichi_SPH project).
+ */
+#ifndef TICHI_SPH_H
+#define TICHI_SPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TSPH_MAX_PHASES 8
+
+/* Return codes.  The reference raises Python exceptions only for configuration
+ * and scenario errors (sph_config.py:13-24, main.py:56,73-74); the host wrapper
+ * maps these codes onto RuntimeError. */
+enum {
+    TSPH_OK = 0,
+    TSPH_ERR_INVALID = 1,   /* bad argument or parameter */
+    TSPH_ERR_CAPACITY = 2,  /* part_num above the capacity given at create */
+    TSPH_ERR_CUDA = 3,      /* a CUDA runtime call failed */
+    TSPH_ERR_STATE = 4      /* call order violated (e.g. stats before a step) */
+};
+
+/* Bits of tsph_stats.status (informational; a step still completes). */
+enum {
+    TSPH_ST_NONFINITE_POS = 1,   /* a position was NaN/inf or its cell overflowed */
+    TSPH_ST_DIV_ITER_CAP = 2,    /* divergence solve stopped at iter_max (main.py:212-213) */
+    TSPH_ST_DENS_ITER_CAP = 4,   /* density solve stopped at iter_max (main.py:233-234) */
+    TSPH_ST_FBM_PASS_CAP = 8,    /* volume-fraction pass loop stopped at fbm_max_passes */
+    TSPH_ST_OUTSIDE_GRID = 16    /* some particle had no valid cell (sph_obj.py:305,319) */
+};
+
+enum { TSPH_DFSPH = 0, TSPH_VFSPH = 1 };
+
+/* Solver constants.  Replaces the `Config` singleton, sph_config.py:83-235.
+ * Values are the f32 values the reference's Taichi fields hold. */
+typedef struct tsph_params {
+    int32_t dim;            /* 2 or 3 (sim_dim) */
+    int32_t phase_num;      /* 1..TSPH_MAX_PHASES */
+    int32_t solver_type;    /* TSPH_DFSPH or TSPH_VFSPH (aliases, sph_obj.py:65-73) */
+    int32_t neighb_range;   /* template half-width r: (2r+1)^dim cells */
+    float part_size;        /* part_size[1] */
+    float kernel_h;         /* kernel_h[1] = 2 * part_size */
+    float kernel_h2;        /* kernel_h[2] */
+    float kernel_sig;       /* kernel_sig[dim] */
+    float lb[3];            /* sim_space_lb */
+    int32_t grid_size[3];   /* ceil((rt - lb) / h) per axis */
+    int64_t node_num;       /* product of grid_size */
+    float gravity[3];
+    float viscosity;        /* dynamic_viscosity */
+    float phase_rest_density[TSPH_MAX_PHASES];
+    float divergence_threshold;
+    float compression_threshold;
+    int32_t iter_min, iter_max;
+    int32_t cs;             /* integer field in the reference */
+    float cfl_factor;
+    float fbm_diffusion, fbm_convection;
+    float surface_tension_gamma;
+    int32_t fbm_enabled;    /* run the volume-fraction block, main.py:244-250 */
+    int32_t fbm_max_passes; /* cap on its pass loop (the reference has none) */
+} tsph_params;
+
+/* Views of one particle set: the fields of `Fluid`, sph_obj.py:24-63, in the
+ * caller's particle order.  Vectors are [capacity][dim] row-major, volume
+ * fractions [capacity][phase_num], drift velocities [capacity][phase_num][dim]. */
+typedef struct tsph_set {
+    int64_t n;              /* part_num[None] */
+    int64_t capacity;       /* max_part_num */
+    float *pos, *vel, *vel_adv, *acce, *acce_adv;
+    float *mass, *rest_density, *rest_volume;
+    float *volume_frac, *volume_frac_tmp;
+    float *W, *sph_density, *sph_compression, *psi_adv;
+    float *alpha, *alpha_1, *alpha_2;
+    float *normal, *drift_vel, *fbm_zeta;
+    int32_t *flag;
+    int32_t *neighb_cell_seq, *neighb_in_cell_seq, *neighb_cell_structured_seq;
+} tsph_set;
+
+/* Host-side copy of the step's scalars (fields `compression`,
+ * `statistics_*_energy` of sph_obj.py:41-47, `config.dt`, and the counters of
+ * GlobalVariable, sph_obj.py:347-360). */
+typedef struct tsph_stats {
+    double dt;
+    double time_count;
+    double compression;
+    double kinetic_energy;
+    double potential_energy;
+    int32_t div_iter;
+    int32_t incom_iter;
+    int32_t fbm_passes;
+    int32_t general_flag;
+    int32_t status;
+    int32_t fluid_in_grid;
+    int32_t bound_in_grid;
+    int32_t steps;
+} tsph_stats;
+
+typedef struct tsph_ctx tsph_ctx;
+
+/* Allocates the solver context: cell grids sized node_num, sorted particle
+ * buffers sized by the capacities, reduction scratch.  Replaces Ngrid()
+ * (sph_obj.py:281-293) plus the solver fields of Fluid.  Returns TSPH_OK. */
+int tsph_create(const tsph_params *params, int64_t fluid_capacity, int64_t bound_capacity,
+                tsph_ctx **out);
+int tsph_destroy(tsph_ctx *ctx);
+
+/* Selects how the two solver loops run: 1 = one CUDA graph per substep with
+ * device-side while nodes (default), 0 = host-driven loops that read the
+ * convergence value every iteration like main.py:201,222. */
+int tsph_set_graph_mode(tsph_ctx *ctx, int use_graph);
+
+/* cfl_condition(fluid), sph.py:41-47: dt on the device.  Also adds dt to the
+ * device clock, as run_step does on the host (main.py:348-349). */
+int tsph_cfl_condition(tsph_ctx *ctx, const tsph_set *fluid, void *stream);
+
+/* sph_step(), main.py:175-256, with the current device dt: grid build,
+ * density/alpha, divergence solve, viscosity, surface tension, density solve,
+ * volume-fraction update when fbm_enabled, mass/position/energy update. */
+int tsph_sph_step(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, void *stream);
+
+/* One substep of run_step (main.py:348-352): cfl_condition, clock, sph_step. */
+int tsph_substep(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, void *stream);
+
+/* Synchronises `stream` and copies the scalars of the last step. */
+int tsph_read_stats(tsph_ctx *ctx, tsph_stats *out, void *stream);
+
+/* Sets the persistent device scalars (clock, dt, the carried-over compression
+ * that the first divergence-loop test reads, main.py:201). */
+int tsph_set_state(tsph_ctx *ctx, double time_count, float dt, double compression, void *stream);
+
+/* Debug / parity: builds the grid for the current positions and writes, per
+ * particle in caller order, the number of neighbours with 0 < r < h among the
+ * fluid ([0]) and the boundary ([1]) set, and an order-independent 64-bit hash
+ * of that neighbour set.  fluid_out: int32[n_f][2] + uint64[n_f]; bound_out the
+ * same for the boundary set.  Synchronises. */
+int tsph_neighbor_stats(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound,
+                        int32_t *fluid_counts, uint64_t *fluid_hash,
+                        int32_t *bound_counts, uint64_t *bound_hash, void *stream);
+
+/* Library version string. */
+const char *tsph_version(void);
+
+/* Text of the last error returned on the calling thread ("" if none). */
+const char *tsph_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TICHI_SPH_H */

@@ -1,0 +1,128 @@
+"""Host-side logic that needs no GPU: configuration, emitters, the C ABI library.
+
+* Config constants equal the oracle's reading of the reference's f32 fields.
+* The emitters reproduce the initial states the reference's own emitters
+  produced (golden ``*.init.npz``) bit for bit.
+* The shared library loads and exports every symbol ``include/tichi_sph.h``
+  declares (no compute call: this runs without a GPU).
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import sph_oracle as O
+from tests import golden_io as G
+from tichi_sph_gb300 import sph_config, _native
+from tichi_sph_gb300.sph_obj import Fluid
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("scene", G.SCENES)
+def test_config_matches_oracle_f32_params(scene):
+    cfg = sph_config.load(*G.paths(scene))
+    p = O.Params.from_files(*G.paths(scene), taichi_f32=True)
+    assert float(cfg.kernel_h[1]) == p.h
+    assert float(cfg.kernel_h[2]) == p.h2
+    assert float(cfg.kernel_sig[cfg.dim[None]]) == p.sig
+    assert cfg.node_num[None] == p.node_num
+    np.testing.assert_array_equal(cfg.neighb_grid_coder[None], p.coder)
+    np.testing.assert_array_equal(cfg.neighb_search_template, p.template)
+    params = cfg.to_params()
+    assert params.node_num == p.node_num
+    assert params.kernel_h == pytest.approx(p.h, rel=0, abs=0)
+
+
+@pytest.mark.parametrize("scene", G.SCENES)
+def test_emitters_reproduce_reference_initial_state(scene):
+    cfg = sph_config.load(*G.paths(scene))
+    init, _ = G.load(scene)
+    objs = {"fluid": Fluid(cfg.fluid_max_part_num[None], cfg, 0, device="cpu"),
+            "bound": Fluid(cfg.bound_max_part_num[None], cfg, 1, device="cpu")}
+    for part in cfg.scenario_buffer:
+        if part == "sim_env":
+            continue
+        for prm in cfg.scenario_buffer[part]["objs"]:
+            o = objs[part]
+            if prm["type"] == "cube":
+                o.scene_add_cube(prm["start_pos"], prm["end_pos"], prm["volume_frac"], prm["vel"],
+                                 int(prm["color"], 16), prm["particle_relaxing_factor"])
+            else:
+                o.scene_add_box(prm["start_pos"], prm["end_pos"], prm["layers"], prm["volume_frac"],
+                                prm["vel"], int(prm["color"], 16), prm["particle_relaxing_factor"])
+    for name, o in objs.items():
+        n = int(init[name + "_n"])
+        assert o.part_num[None] == n
+        for f in ("pos", "vel", "rest_volume"):
+            np.testing.assert_array_equal(getattr(o, f)[:n].numpy(), init[name + "_" + f], err_msg=f)
+        if scene not in G.FBM_SCENES:  # VFSPH scenes carry harness-added volume-fraction noise
+            for f in ("volume_frac", "rest_density", "mass"):
+                np.testing.assert_array_equal(getattr(o, f)[:n].numpy(), init[name + "_" + f], err_msg=f)
+
+
+def test_capacity_overflow_raises():
+    cfg = sph_config.load(*G.paths("dfsph2d"))
+    f = Fluid(10, cfg, 0, device="cpu")
+    with pytest.raises(Exception, match="exceed max_part_num"):
+        f.scene_add_cube([0, 0], [0.5, 0.5], [1], [0, 0], 0, 1.0)
+
+
+def test_bad_config_raises():
+    cfg_path, scen_path = G.paths("dfsph2d")
+    import json
+    cfgd = json.load(open(cfg_path))
+    scen = json.load(open(scen_path))
+    del cfgd["solver_cs"]
+    with pytest.raises(Exception, match="solver_cs"):
+        sph_config.Config(cfgd, scen)
+    cfgd = json.load(open(cfg_path))
+    cfgd["solver_type"] = "WCSPH"
+    with pytest.raises(Exception, match="solver_type"):
+        sph_config.Config(cfgd, scen)
+
+
+def test_argv_parsing_accepts_both_spellings():
+    assert sph_config.parse_args(["-c", "a.json", "-s", "b.json"]) == ("a.json", "b.json")
+    assert sph_config.parse_args(["--configFile=a", "--scenarioFile=b"]) == ("a", "b")
+
+
+def _declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for fn in os.listdir(inc):
+        if fn.endswith(".h"):
+            src = open(os.path.join(inc, fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(tsph_[a-z_0-9]+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    from tichi_sph_gb300 import build
+    path = build.build()
+    L = ctypes.CDLL(path)
+    declared = _declared_symbols()
+    assert "tsph_sph_step" in declared and "tsph_create" in declared
+    for name in sorted(declared):
+        assert hasattr(L, name), name
+    # the ctypes signature table covers the same set
+    assert declared == set(_native.SIGNATURES), declared ^ set(_native.SIGNATURES)
+
+
+def test_struct_layouts_match_header():
+    # tsph_params / tsph_set / tsph_stats sizes as laid out by the C compiler
+    import subprocess
+    import tempfile
+    src = ('#include <stdio.h>\n#include "tichi_sph.h"\n'
+           'int main(){printf("%zu %zu %zu\\n", sizeof(tsph_params), sizeof(tsph_set), sizeof(tsph_stats));return 0;}\n')
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "t")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert [int(x) for x in out] == [ctypes.sizeof(_native.Params), ctypes.sizeof(_native.Set),
+                                    ctypes.sizeof(_native.Stats)]

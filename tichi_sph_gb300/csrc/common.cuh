@@ -1,0 +1,213 @@
+// Internal definitions shared by the CUDA translation units of the SPH hot path.
+//
+// Data layout (all in HBM, owned by tsph_ctx):
+//   * two cell grids (fluid, boundary) over the reference's linear cell codes
+//     code = x + nx*y + nx*ny*z (sph_config.py:210-214): count[node_num] and the
+//     exclusive scan start[node_num + 1];
+//   * per set, a permutation perm[sorted slot] = particle id, sorted by cell code
+//     with ties broken by particle id; particles without a valid cell sit after
+//     the in-grid ones (they still run their own sums, sph.py:52, but are never
+//     found as neighbours, sph_obj.py:305,319);
+//   * sorted SoA copies of the per-particle state as float4 (x, y, z, X) etc., so
+//     a neighbour cell row (three x-adjacent cells) is one contiguous, coalesced
+//     range of 16-byte loads.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/tichi_sph.h"
+
+namespace tsph {
+
+constexpr int kBlock = 256;     // threads per block of the particle sweeps
+constexpr int kMaxP = TSPH_MAX_PHASES;
+
+// Scalars that persist across steps (device resident).
+struct DevPersist {
+    double time_count;
+    double compression;  // carried into the next divergence-loop test (main.py:201)
+    float dt;
+    int32_t steps;
+};
+
+// Scalars of one step; zeroed by a memset at the start of every step.
+struct DevStep {
+    unsigned int vmax_bits;     // max |v| over fluid (float bits, non-negative)
+    int32_t cur;                // which v_adv buffer is current
+    int32_t iter;               // iteration counter of the running solve
+    int32_t cond;               // loop condition (mirrors the graph conditional)
+    int32_t div_iter, incom_iter;
+    int32_t fbm_pass, general_flag, fbm_passes, fbm_cond;
+    int32_t f_tail, b_tail;     // particles without a valid cell
+    int32_t status;
+    int32_t gflag_out;          // general_flag after the last volume-fraction pass
+    unsigned int ticket[8];
+    double kinetic_energy, potential_energy;
+};
+
+// Launch-time constants of one context (passed by value: lands in the constant bank).
+struct KConst {
+    float lb[3];
+    float h, h2, inv_h, sig, sig_h;   // sig_h = sig / h
+    long long node_num, nx, nxny;
+    int R;                            // neighb_range
+    int dim, P, vfsph;
+    float g[3];
+    float mu, gamma, fbm_c, fbm_D;
+    float rho_phase[kMaxP];
+    float part_size, cfl;
+    int cs, iter_min, iter_max, fbm_max_passes;
+    float div_tol, comp_tol;
+    float c_coh;                      // 32 / (pi h^3), cohesion normaliser
+};
+
+struct FluidBuf {
+    int64_t cap;
+    int *count, *start, *slot, *perm, *inv;
+    float4 *pos;       // x, y, z, X (mass for DFSPH, rest_volume for VFSPH)
+    float2 *mv;        // mass, rest_volume
+    float4 *mpsi;      // mass, psi (sph_psi), psi0 (rest_psi), alpha
+    float *rho0;       // rest_density
+    float4 *vel;       // velocity after the divergence solve
+    float4 *vadv;      // two buffers of cap: v_adv ping-pong
+    float *psiadv, *kappa;   // psi_adv and psi_adv / alpha
+    float4 *acc;       // acce_adv
+    float4 *normal;
+    float *W, *rho, *comp, *a2;
+    float4 *a1;
+    float *vf, *vftmp;       // [P][cap]
+    float4 *drift;           // [P][cap]
+    float4 *facc;            // acce (fbm_acce)
+    float *zeta;
+    int *flagpass;           // 0 = unflagged, else the FBM pass that flagged it
+};
+
+struct BoundBuf {
+    int64_t cap;
+    int *count, *start, *slot, *perm, *inv;
+    float4 *pos;       // x, y, z, X
+    float2 *mv;        // mass, rest_volume
+    float4 *vadv;      // boundary vel_adv (never advanced by the reference)
+    float *kappa;      // psi_adv / alpha of the boundary particle
+    float *W, *rho, *comp, *a2, *alpha;
+};
+
+struct Scratch {
+    double *partials;        // per-block FP64 partial sums
+    int64_t partials_len;
+    int *scan_blocks;        // block totals of the cell scans
+    int64_t scan_len;
+};
+
+// ---------------------------------------------------------------------------------
+// Kernel functions of the reference, sph_util.py:4-43 (q = r / h).
+__device__ __forceinline__ float kw(float q) {
+    float a = 6.f * (q * q * q - q * q) + 1.f;
+    float b = 1.f - q;
+    return q <= 0.5f ? a : (q < 1.f ? 2.f * b * b * b : 0.f);
+}
+__device__ __forceinline__ float kwg(float q) {
+    float a = 6.f * (3.f * q * q - 2.f * q);
+    float b = 1.f - q;
+    return q <= 0.5f ? a : (q < 1.f ? -6.f * b * b : 0.f);
+}
+__device__ __forceinline__ float kcoh(float q) {
+    float b = 1.f - q;
+    float t = b * b * b * q * q * q;
+    return q <= 0.5f ? 2.f * t - 1.f / 64.f : (q < 1.f ? t : 0.f);
+}
+
+// Cell of a position: floor((p - lb) / h) per axis with IEEE division
+// (sph_util.py:65-67), and the linear code (sph_util.py:70-72).  `ok` is false for
+// a non-finite position or a coordinate beyond +-2^40 cells.
+template <int DIM>
+__device__ __forceinline__ long long cell_code(float4 p, const KConst &k, bool &ok) {
+    const float c[3] = {p.x, p.y, p.z};
+    long long s[3] = {0, 0, 0};
+    ok = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        float f = floorf(__fdiv_rn(c[d] - k.lb[d], k.h));
+        if (!(f > -1.0e12f && f < 1.0e12f)) ok = false;
+        s[d] = ok ? (long long)f : 0;
+    }
+    long long code = s[0] + s[1] * k.nx;
+    if (DIM == 3) code += s[2] * k.nxny;
+    return code;
+}
+
+// Visits every candidate the reference's template loop visits (sph.py:52-60):
+// for each row offset (dy, dz) the x-adjacent codes [rc - R, rc + R] clipped to
+// the valid range (0, node_num) form one contiguous range of sorted slots.
+// Codes are linear, so an x offset past a row end continues into the next row
+// exactly like dim_encode without bounds checks.
+template <int DIM, class F>
+__device__ __forceinline__ void visit_candidates(const int *__restrict__ start, const KConst &k,
+                                                 long long code, F &&f) {
+    const int R = k.R;
+    const int zr = (DIM == 3) ? R : 0;
+    for (int dz = -zr; dz <= zr; ++dz) {
+        for (int dy = -R; dy <= R; ++dy) {
+            long long rc = code + dy * k.nx + dz * k.nxny;
+            long long lo = rc - R, hi = rc + R;
+            if (lo < 1) lo = 1;
+            if (hi > k.node_num - 1) hi = k.node_num - 1;
+            if (lo > hi) continue;
+            const int beg = __ldg(start + lo);
+            const int end = __ldg(start + hi + 1);
+            for (int j = beg; j < end; ++j) f(j);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Deterministic block reduction in FP64 (warp shuffles, fixed tree).
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int BS>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = (lane < BS / 32) ? sh[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;  // valid in thread 0
+}
+
+// True (in every thread) for the block that finishes last; the caller's per-block
+// results must already be stored.  Classic fence + ticket pattern: no thread ever
+// waits on another block.
+__device__ __forceinline__ bool last_block_done(unsigned int *ticket) {
+    __shared__ bool am_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int t = atomicAdd(ticket, 1u);
+        am_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (am_last) __threadfence();
+    return am_last;
+}
+
+// Sums partials[0..n) in a fixed order within one block (result in thread 0).
+template <int BS>
+__device__ __forceinline__ double sum_partials(const double *partials, int n, double *sh) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += BS) v += __ldcg(partials + i);
+    return block_sum<BS>(v, sh);
+}
+
+inline int blocks_for(int64_t n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
+
+}  // namespace tsph

@@ -1,0 +1,52 @@
+// Solver context and the host-side launchers of each kernel group.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+struct tsph_ctx {
+    tsph_params p;
+    tsph::KConst k;
+    tsph::FluidBuf F;
+    tsph::BoundBuf B;
+    tsph::Scratch S;
+    tsph::DevPersist *dp;
+    tsph::DevStep *ds;
+    tsph::DevStep *host_ds;    // pinned mirror for host-loop mode and stats
+    tsph::DevPersist *host_dp;
+    int use_graph;
+    int stepped;
+    // cached per-substep graph, keyed on the particle counts and array pointers
+    cudaGraphExec_t exec;
+    unsigned long long graph_key[4];
+    int graph_substep;         // whether the cached graph includes cfl_condition
+};
+
+namespace tsph {
+
+enum SolveKind { kSolveDiv = 0, kSolveDens = 1 };
+
+// grid.cu
+void launch_step_begin(tsph_ctx &c, cudaStream_t st);
+void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st);
+void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);
+void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);
+void launch_neighbor_stats(tsph_ctx &c, int64_t nf, int64_t nb, int32_t *fc, uint64_t *fh,
+                           int32_t *bc, uint64_t *bh, cudaStream_t st);
+
+// sweeps.cu
+void launch_density(tsph_ctx &c, int64_t nf, int64_t nb, cudaStream_t st);
+void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond,
+                        cudaStream_t st);
+void launch_solve_iter(tsph_ctx &c, int64_t nf, int kind, cudaGraphConditionalHandle h,
+                       int use_cond, cudaStream_t st);
+void launch_advect(tsph_ctx &c, int64_t nf, cudaStream_t st);
+
+// fbm.cu
+void launch_fbm_begin(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond,
+                      cudaStream_t st);
+void launch_fbm_pass(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond,
+                     cudaStream_t st);
+
+}  // namespace tsph

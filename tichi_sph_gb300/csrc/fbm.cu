@@ -1,0 +1,190 @@
+// VFSPH volume-fraction update (the reference's "FBM" block), sph.py:301-379,
+// driven as in main.py:244-250 (commented out there; enabled by fbm_enabled):
+//
+//   while general_flag:
+//       clean_tmp; convect (drift velocities + convective flux); diffuse; check_tmp
+//   update_volume_frac
+//
+// The drift velocities depend only on the step's velocities and volume
+// fractions, which no pass changes, so they are computed once.  A pass sums the
+// convective and diffusive flux of each unflagged particle over its unflagged
+// neighbours and flags it if any phase would go negative; flags set during pass
+// p (value p) do not exclude a neighbour until pass p + 1, which is what the
+// reference's separate check kernel achieves.  The number of passes is capped
+// (fbm_max_passes); the reference loops forever if a flagged particle's own
+// volume fraction is already negative.
+#include <cuda_runtime.h>
+
+#include "ctx.h"
+
+namespace tsph {
+
+__global__ void k_fbm_begin(DevStep *ds, cudaGraphConditionalHandle h, int use_cond) {
+    ds->fbm_pass = 0;
+    ds->general_flag = 0;
+    ds->fbm_cond = 1;  // SPH_clean_value sets general_flag = 1: at least one pass
+    if (use_cond) cudaGraphSetConditional(h, 1u);
+}
+
+// First loop of SPH_FBM_convect, sph.py:331-345.
+template <int DIM, int P>
+__global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F, int64_t n, const DevStep *ds,
+                                                      const DevPersist *dp) {
+    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (s >= n) return;
+    const float dt = dp->dt;
+    const float4 va = F.vadv[ds->cur * F.cap + s];
+    const float4 v = F.vel[s];
+    const float ax = (va.x - v.x) / dt, ay = (va.y - v.y) / dt, az = (va.z - v.z) / dt;
+    const float rho0 = F.rho0[s];
+    float vf[P];
+    float zeta = 0.f;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        vf[q] = F.vf[q * F.cap + s];
+        zeta += vf[q] * (k.rho_phase[q] - rho0) / k.rho_phase[q];
+    }
+    const float gz = DIM == 3 ? k.g[2] : 0.f;
+    const float fx = (ax - zeta * k.g[0]) / (1.f - zeta);
+    const float fy = (ay - zeta * k.g[1]) / (1.f - zeta);
+    const float fz = (az - zeta * gz) / (1.f - zeta);
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        const float c = vf[q] * (k.rho_phase[q] - rho0);
+        float dx = c * (k.g[0] - fx), dy = c * (k.g[1] - fy), dz = c * (gz - fz);
+        const float w = vf[q] * k.rho_phase[q];
+        if (w > 1e-6f) {
+            dx /= w; dy /= w; dz /= w;
+        } else {
+            dx *= 0.f; dy *= 0.f; dz *= 0.f;
+        }
+        dx += fx - ax; dy += fy - ay; dz += fz - az;
+        F.drift[q * F.cap + s] = make_float4(dx * dt, dy * dt, dz * dt, 0.f);
+    }
+    F.acc[s] = make_float4(ax, ay, az, 0.f);
+    F.facc[s] = make_float4(fx, fy, fz, 0.f);
+    F.zeta[s] = zeta;
+}
+
+// One pass: SPH_FBM_clean_tmp + pair loop of SPH_FBM_convect + SPH_FBM_diffuse +
+// SPH_FBM_check_tmp (sph.py:301-372).  The last block evaluates the loop test.
+template <int DIM, int P>
+__global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, int64_t n, DevStep *ds,
+                                                     const DevPersist *dp, cudaGraphConditionalHandle h,
+                                                     int use_cond) {
+    __shared__ int any_neg;
+    if (threadIdx.x == 0) any_neg = 0;
+    __syncthreads();
+    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    const int pass = ds->fbm_pass + 1;
+    if (s < n) {
+        const int fp = F.flagpass[s];
+        float tmp[P];
+        float vfi[P];
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            tmp[q] = 0.f;
+            vfi[q] = F.vf[q * F.cap + s];
+        }
+        if (fp == 0) {
+            const float dt = dp->dt;
+            const float4 pi = F.pos[s];
+            float4 ui[P];
+#pragma unroll
+            for (int q = 0; q < P; ++q) ui[q] = F.drift[q * F.cap + s];
+            const float cc = k.fbm_c * dt, cd = dt * k.fbm_D, eps = 0.01f * k.h2;
+            bool ok;
+            const long long code = cell_code<DIM>(pi, k, ok);
+            if (ok) {
+                visit_candidates<DIM>(F.start, k, code, [&](int j) {
+                    const float4 pj = F.pos[j];
+                    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (!(r2 < k.h2 && r2 > 0.f)) return;
+                    const int fj = F.flagpass[j];
+                    if (fj != 0 && fj != pass) return;
+                    const float r = sqrtf(r2);
+                    const float wg = kwg(r * k.inv_h) * k.sig_h;
+                    const float Vj = F.mv[j].y;
+                    const float gx = dx / r * wg, gy = dy / r * wg, gz = dz / r * wg;
+                    const float dif = cd * Vj * r * wg / (r2 + eps);
+#pragma unroll
+                    for (int q = 0; q < P; ++q) {
+                        const float vfj = F.vf[q * F.cap + j];
+                        const float4 uj = F.drift[q * F.cap + j];
+                        const float fx = vfi[q] * ui[q].x + vfj * uj.x;
+                        const float fy = vfi[q] * ui[q].y + vfj * uj.y;
+                        const float fz = vfi[q] * ui[q].z + vfj * uj.z;
+                        tmp[q] -= cc * Vj * (fx * gx + fy * gy + fz * gz);
+                        tmp[q] += (vfi[q] - vfj) * dif;
+                    }
+                });
+            }
+        }
+        bool neg = false;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            F.vftmp[q * F.cap + s] = tmp[q];
+            if (vfi[q] + tmp[q] < 0.f) neg = true;
+        }
+        if (neg) {
+            if (fp == 0) F.flagpass[s] = pass;
+            any_neg = 1;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && any_neg) atomicExch(&ds->general_flag, 1);
+    if (last_block_done(&ds->ticket[3])) {
+        if (threadIdx.x == 0) {
+            const int gf = atomicAdd(&ds->general_flag, 0);
+            ds->fbm_pass = pass;
+            ds->fbm_passes = pass;
+            ds->gflag_out = gf;
+            const int cond = gf && pass < k.fbm_max_passes;
+            if (gf && !cond) ds->status |= TSPH_ST_FBM_PASS_CAP;
+            ds->fbm_cond = cond;
+            ds->general_flag = 0;
+            ds->ticket[3] = 0;
+            if (use_cond) cudaGraphSetConditional(h, cond ? 1u : 0u);
+        }
+    }
+}
+
+template <int P>
+static void fbm_pass_dim(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st,
+                         bool drift) {
+    const int nb = blocks_for(nf) > 0 ? blocks_for(nf) : 1;
+    if (c.k.dim == 3) {
+        if (drift) k_fbm_drift<3, P><<<nb, kBlock, 0, st>>>(c.k, c.F, nf, c.ds, c.dp);
+        else k_fbm_pass<3, P><<<nb, kBlock, 0, st>>>(c.k, c.F, nf, c.ds, c.dp, h, use_cond);
+    } else {
+        if (drift) k_fbm_drift<2, P><<<nb, kBlock, 0, st>>>(c.k, c.F, nf, c.ds, c.dp);
+        else k_fbm_pass<2, P><<<nb, kBlock, 0, st>>>(c.k, c.F, nf, c.ds, c.dp, h, use_cond);
+    }
+}
+
+static void fbm_dispatch(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st,
+                         bool drift) {
+    switch (c.k.P) {
+        case 1: fbm_pass_dim<1>(c, nf, h, use_cond, st, drift); break;
+        case 2: fbm_pass_dim<2>(c, nf, h, use_cond, st, drift); break;
+        case 3: fbm_pass_dim<3>(c, nf, h, use_cond, st, drift); break;
+        case 4: fbm_pass_dim<4>(c, nf, h, use_cond, st, drift); break;
+        case 5: fbm_pass_dim<5>(c, nf, h, use_cond, st, drift); break;
+        case 6: fbm_pass_dim<6>(c, nf, h, use_cond, st, drift); break;
+        case 7: fbm_pass_dim<7>(c, nf, h, use_cond, st, drift); break;
+        default: fbm_pass_dim<8>(c, nf, h, use_cond, st, drift); break;
+    }
+}
+
+void launch_fbm_begin(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+    cudaMemsetAsync(c.F.flagpass, 0, sizeof(int) * (nf > 0 ? nf : 1), st);
+    if (nf > 0) fbm_dispatch(c, nf, 0, 0, st, true);
+    k_fbm_begin<<<1, 1, 0, st>>>(c.ds, h, use_cond);
+}
+
+void launch_fbm_pass(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+    fbm_dispatch(c, nf, h, use_cond, st, false);
+}
+
+}  // namespace tsph

@@ -1,0 +1,242 @@
+"""Headless driver: scenario set-up, the time loop and per-frame output.
+
+Mirrors ``main.py`` of Tichi_SPH without its GGUI window (there is no graphics
+stack here): the objects of ``main.py:8-14``, the scenario system of
+``main.py:16-112`` (cubes, boxes, PLY point clouds, inlets and objects delayed
+by ``time``), ``run_step`` (``main.py:339-368``) and the output writers
+(``main.py:115-171``, ``371-378``) with portable paths.
+"""
+import json
+import os
+import time
+import warnings
+
+import numpy as np
+
+from .sph import Solver
+from .sph_obj import Fluid, GlobalVariable, Ngrid
+
+
+def warn(*message):
+    """``sph_util.py:77-80``."""
+    warnings.warn("".join(str(m) for m in message), RuntimeWarning)
+
+
+def read_ply(path):
+    """ASCII PLY vertex reader (``sph_util.py:83-87`` reads x, y, z of each vertex)."""
+    with open(path, "rb") as f:
+        header = []
+        while True:
+            line = f.readline().decode("ascii", errors="replace").strip()
+            header.append(line)
+            if line == "end_header":
+                break
+            if not line and len(header) > 200:
+                raise ValueError("bad PLY header in %s" % path)
+        nvert, props, fmt = 0, [], "ascii"
+        in_vertex = False
+        for ln in header:
+            t = ln.split()
+            if not t:
+                continue
+            if t[0] == "format":
+                fmt = t[1]
+            elif t[0] == "element":
+                in_vertex = t[1] == "vertex"
+                if in_vertex:
+                    nvert = int(t[2])
+            elif t[0] == "property" and in_vertex:
+                props.append(t[-1])
+        if fmt != "ascii":
+            raise ValueError("only ASCII PLY is supported (%s)" % path)
+        rows = [f.readline().split() for _ in range(nvert)]
+    ix = [props.index(a) for a in ("x", "y", "z")]
+    return np.array([[float(r[i]) for i in ix] for r in rows])
+
+
+def write_ply(path, frame_num, dim, num, pos):
+    """``sph_util.py:90-100``: ASCII PLY of the first ``num`` positions."""
+    with open(str(path) + "_" + str(frame_num) + ".ply", "w") as f:
+        f.write("ply\nformat ascii 1.0\nelement vertex %d\nproperty float x\nproperty float y\n"
+                "property float z\nend_header\n" % num)
+        for i in range(num):
+            z = pos[i, 2] if dim == 3 else 0.0
+            f.write("%s %s %s\n" % (np.float32(pos[i, 0]), np.float32(pos[i, 1]), np.float32(z)))
+
+
+class Simulation:
+    """The reference's module-level state of ``main.py`` as one object."""
+
+    def __init__(self, config, fbm=False, use_graph=True, device=None, out_dir=None):
+        self.config = config
+        self.ngrid = Ngrid(config)
+        self.fluid = Fluid(config.fluid_max_part_num[None], config, uid=0, device=device)
+        self.bound = Fluid(config.bound_max_part_num[None], config, uid=1, device=device)
+        self.globalvar = GlobalVariable()
+        self.scenario_wait_buffer = []
+        self.inlets = []
+        self.fbm = fbm
+        self.use_graph = use_graph
+        self.out_dir = out_dir or config.solver_type
+        self._solver = None
+
+    @property
+    def solver(self):
+        if self._solver is None:
+            self._solver = Solver(self.config, self.fluid, self.bound, fbm=self.fbm, use_graph=self.use_graph)
+        return self._solver
+
+    # ---------------------------------------------------------------- scenario
+    def get_obj_from_str(self, s):
+        """``main.py:16-23``."""
+        if s == "fluid":
+            return self.fluid
+        if s == "bound":
+            return self.bound
+        print("scenario WARNING: object does not exist (name:", s, ")")
+        return None
+
+    def inlet_helper_get_dt(self, norm, speed, relaxing_factor):
+        """``main.py:26-39``."""
+        norm = np.array(norm) / np.linalg.norm(np.array(norm))
+        if speed < 0:
+            norm, speed = -norm, -speed
+        acc = np.dot(norm, self.config.gravity[None].astype(np.float64))
+        r = float(self.config.part_size[1])
+        if acc < 1e-6:
+            if speed > 0:
+                return r * relaxing_factor / speed
+            return float("inf")
+        return ((speed ** 2 + 2 * acc * r) ** 0.5 - speed) / acc * relaxing_factor
+
+    def add_to_scenario(self, obj_str, param):
+        """``main.py:42-60``."""
+        obj = self.get_obj_from_str(obj_str)
+        if obj is None:
+            print("scenario WARNING: obj '", obj_str, "' non-exist.")
+            return
+        t = param["type"]
+        if t == "cube":
+            obj.scene_add_cube(param["start_pos"], param["end_pos"], param["volume_frac"], param["vel"],
+                               int(param["color"], 16), param["particle_relaxing_factor"])
+        elif t == "box":
+            obj.scene_add_box(param["start_pos"], param["end_pos"], param["layers"], param["volume_frac"],
+                              param["vel"], int(param["color"], 16), param["particle_relaxing_factor"])
+        elif t == "ply":
+            verts = read_ply(param["file_name"].replace("\\", os.sep))
+            obj.push_part_from_ply(len(verts), verts, param["volume_frac"], param["vel"], int(param["color"], 16))
+        elif t == "inlet":
+            if np.linalg.norm(np.array(param["norm"])) < 1e-6:
+                raise Exception("inlet ERROR: magnitute of attribute 'norm' should not be zero.")
+            param["obj"] = obj_str
+            param["dt"] = self.inlet_helper_get_dt(param["norm"], param["speed"], param["particle_relaxing_factor"])
+            param["t_pre"] = self.globalvar.time_count - param["dt"]
+            self.inlets.append(param)
+
+    def init_scenario(self):
+        """``main.py:62-79`` (the GGUI-only calls are dropped)."""
+        try:
+            for part in self.config.scenario_buffer:
+                if part != "sim_env":
+                    for param in self.config.scenario_buffer[part]["objs"]:
+                        if "time" not in param or param["time"] <= 0.0:
+                            self.add_to_scenario(part, param)
+                        else:
+                            param["_part"] = part
+                            self.scenario_wait_buffer.append(param)
+        except Exception as e:
+            raise Exception("scenario ERROR: no scenario file or scenario file invalid.") from e
+
+    def refresh_inlets(self):
+        """``main.py:81-100``."""
+        gv = self.globalvar
+        for i in range(len(self.inlets) - 1, -1, -1):
+            inlet = self.inlets[i]
+            if "end_time" in inlet and gv.time_count >= inlet["end_time"]:
+                self.inlets.pop(i)
+            elif gv.time_count >= inlet["t_pre"] + inlet["dt"]:
+                try:
+                    inlet["t_pre"] = gv.time_count
+                    self.get_obj_from_str(inlet["obj"]).scene_add_from_inlet(
+                        inlet["center"], inlet["size"], inlet["norm"], inlet["speed"], inlet["volume_frac"],
+                        int(inlet["color"], 16), inlet["particle_relaxing_factor"])
+                except Exception:
+                    warn("inlet WARNING: refresh_inlets failed for:", json.dumps(inlet))
+                    self.inlets.pop(i)
+
+    def refresh_scenario(self):
+        """``main.py:102-112``."""
+        for i in range(len(self.scenario_wait_buffer) - 1, -1, -1):
+            param = self.scenario_wait_buffer[i]
+            try:
+                if param["time"] <= self.globalvar.time_count:
+                    self.add_to_scenario(param["_part"], param)
+                    self.scenario_wait_buffer.pop(i)
+            except Exception:
+                warn("scenario WARNING: invalid scenario object:", json.dumps(param))
+                self.scenario_wait_buffer.pop(i)
+        self.refresh_inlets()
+
+    # ---------------------------------------------------------------- time loop
+    def substep(self):
+        """One substep of run_step (main.py:347-352): the clock and counters are
+        read back once per substep (the time loop needs dt on the host)."""
+        self.refresh_scenario()
+        s = self.solver
+        s.substep()
+        st = s.stats()
+        gv = self.globalvar
+        gv.time_count += st["dt"]
+        gv.div_iter_count = st["div_iter"]
+        gv.incom_iter_count = st["incom_iter"]
+        gv.frame_div_iter += gv.div_iter_count
+        gv.frame_incom_iter += gv.incom_iter_count
+        gv.step_counter += 1
+        return st
+
+    def run_step(self, verbose=False):
+        """``main.py:339-368``: advance to the next frame at ``gui_fps``."""
+        gv = self.globalvar
+        gv.time_counter += 1
+        while gv.time_count < gv.time_counter / self.config.gui_fps[None]:
+            if gv.is_first_time:
+                gv.time_start = time.time()
+                gv.is_first_time = False
+            self.substep()
+        gv.time_real = time.time() - gv.time_start
+        if verbose:
+            print("current time: ", gv.time_count)
+            print("---------------------real time------------------------", gv.time_real)
+            print("time step: ", self.config.dt[None])
+
+    # ---------------------------------------------------------------- output
+    def frame_record(self):
+        """Contents of ``write_full_json`` (main.py:151-171)."""
+        gv = self.globalvar
+        ke = self.fluid.statistics_kinetic_energy[None]
+        pe = self.fluid.statistics_gravity_potential_energy[None]
+        return {
+            "step": gv.step_counter, "frame": gv.time_counter, "timeInSimulation": gv.time_count,
+            "timeStep": self.config.dt[None], "fps": self.config.gui_fps[None],
+            "iteration": {"divergenceFree_iteration": gv.frame_div_iter,
+                          "incompressible_iteration": gv.frame_incom_iter,
+                          "sum_iteration": gv.frame_div_iter + gv.frame_incom_iter},
+            "energy": {"statistics_kinetic_energy": ke, "statistics_gravity_potential_energy": pe,
+                       "sum_energy": ke + pe},
+        }
+
+    def write_files(self):
+        """``main.py:371-378`` without the PNG: PLY of fluid positions, frame JSON,
+        npy of positions and velocities."""
+        d = self.config.dim[None]
+        n = self.fluid.part_num[None]
+        frame = self.globalvar.time_counter
+        for sub in ("ply", "json", "part_data"):
+            os.makedirs(os.path.join(self.out_dir, sub), exist_ok=True)
+        pos = self.fluid.pos[:n].cpu().numpy()
+        vel = self.fluid.vel[:n].cpu().numpy()
+        write_ply(os.path.join(self.out_dir, "ply", "fluid_pos"), frame, d, n, pos)
+        with open(os.path.join(self.out_dir, "json", "frame%d.json" % frame), "w") as f:
+            f.write(json.dumps(self.frame_record()))
+        np.save(os.path.join(self.out_dir, "part_data", "vel_%d" % frame), vel)
+        np.save(os.path.join(self.out_dir, "part_data", "pos_%d" % frame), pos)

@@ -1,0 +1,130 @@
+"""The solver: the reference's per-substep kernels behind one CUDA context.
+
+``sph.py`` of Tichi_SPH exposes ~27 Taichi kernels that ``main.py:175-256``
+(``sph_step``) calls in a fixed order.  Here that whole sequence is one call of
+the C ABI (``tsph_sph_step`` / ``tsph_substep``), replayed as a CUDA graph with
+device-side solver loops.  :class:`Solver` owns the context; the module-level
+``cfl_condition`` / ``sph_step`` mirror the reference's entry points.
+"""
+import torch
+
+from . import _native
+from ._native import check
+
+
+def _stream_handle(device):
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+class Solver:
+    """One solver context for a (fluid, boundary) pair of particle sets.
+
+    ``fbm`` enables the volume-fraction update block that the reference ships
+    commented out (``main.py:244-250``); ``use_graph=False`` runs the solver loops
+    host-driven, reading the convergence value every iteration as the reference
+    does (``main.py:201,222``)."""
+
+    def __init__(self, config, fluid, bound, fbm=False, use_graph=True, fbm_max_passes=1000):
+        if fluid.device.type != "cuda" or bound.device.type != "cuda":
+            raise RuntimeError("tichi_sph_gb300: particle sets must live on a CUDA device")
+        self.config = config
+        self.fluid = fluid
+        self.bound = bound
+        self.fbm = bool(fbm)
+        self.device = fluid.device
+        L = _native.lib()
+        self._lib = L
+        params = config.to_params(fbm_enabled=self.fbm, fbm_max_passes=fbm_max_passes)
+        ctx = _native.CtxP()
+        with torch.cuda.device(self.device):
+            check(L.tsph_create(_native.C.byref(params), fluid.max_part_num, bound.max_part_num,
+                                _native.C.byref(ctx)), "tsph_create")
+        self.ctx = ctx
+        self.set_graph_mode(use_graph)
+        self._stats = _native.Stats()
+
+    def set_graph_mode(self, use_graph):
+        check(self._lib.tsph_set_graph_mode(self.ctx, 1 if use_graph else 0), "tsph_set_graph_mode")
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self._lib.tsph_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _sets(self):
+        return _native.C.byref(self.fluid.native_set()), _native.C.byref(self.bound.native_set())
+
+    def cfl_condition(self):
+        """``cfl_condition(fluid)``, sph.py:41-47 (dt stays on the device)."""
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_cfl_condition(self.ctx, _native.C.byref(self.fluid.native_set()),
+                                               _native.C.c_void_p(_stream_handle(self.device))),
+                  "tsph_cfl_condition")
+
+    def sph_step(self):
+        """``sph_step()``, main.py:175-256, with the current dt."""
+        f, b = self._sets()
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_sph_step(self.ctx, f, b, _native.C.c_void_p(_stream_handle(self.device))),
+                  "tsph_sph_step")
+
+    def substep(self):
+        """cfl_condition + clock + sph_step (main.py:348-350) as one graph launch."""
+        f, b = self._sets()
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_substep(self.ctx, f, b, _native.C.c_void_p(_stream_handle(self.device))),
+                  "tsph_substep")
+
+    def set_state(self, time_count=0.0, dt=0.0, compression=0.0):
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_set_state(self.ctx, float(time_count), float(dt), float(compression),
+                                           _native.C.c_void_p(_stream_handle(self.device))), "tsph_set_state")
+
+    def stats(self):
+        """Synchronises and returns the step's scalars; also refreshes the
+        reference-visible scalars (``config.dt[None]``, ``fluid.compression[None]``,
+        ``fluid.statistics_*_energy[None]``, ``fluid.general_flag[None]``)."""
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_read_stats(self.ctx, _native.C.byref(self._stats),
+                                            _native.C.c_void_p(_stream_handle(self.device))), "tsph_read_stats")
+        s = self._stats
+        self.config.dt[None] = s.dt
+        self.fluid.compression[None] = s.compression
+        self.fluid.statistics_kinetic_energy[None] = s.kinetic_energy
+        self.fluid.statistics_gravity_potential_energy[None] = s.potential_energy
+        self.fluid.general_flag[None] = s.general_flag
+        return {k: getattr(s, k) for k, _ in _native.Stats._fields_}
+
+    def neighbor_stats(self):
+        """Per-particle neighbour counts (fluid, boundary) and set hashes."""
+        nf, nb = self.fluid.part_num[None], self.bound.part_num[None]
+        dev = self.device
+        fc = torch.zeros((max(nf, 1), 2), dtype=torch.int32, device=dev)
+        bc = torch.zeros((max(nb, 1), 2), dtype=torch.int32, device=dev)
+        fh = torch.zeros(max(nf, 1), dtype=torch.int64, device=dev)
+        bh = torch.zeros(max(nb, 1), dtype=torch.int64, device=dev)
+        f, b = self._sets()
+        u64p = _native.C.POINTER(_native.C.c_uint64)
+        with torch.cuda.device(dev):
+            check(self._lib.tsph_neighbor_stats(
+                self.ctx, f, b,
+                _native.C.cast(fc.data_ptr(), _native._ip), _native.C.cast(fh.data_ptr(), u64p),
+                _native.C.cast(bc.data_ptr(), _native._ip), _native.C.cast(bh.data_ptr(), u64p),
+                _native.C.c_void_p(_stream_handle(dev))), "tsph_neighbor_stats")
+        return fc[:nf], fh[:nf], bc[:nb], bh[:nb]
+
+
+def cfl_condition(solver):
+    """Module-level form of ``cfl_condition(fluid)`` (sph.py:41-47)."""
+    solver.cfl_condition()
+
+
+def sph_step(solver):
+    """Module-level form of ``sph_step()`` (main.py:175-256)."""
+    solver.sph_step()
