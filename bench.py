@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Throughput of the SPH substep (particle-steps/s) on the GPU, and the reference arm.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the 3D single-phase DFSPH dam break (``workloads.dambreak_3d``): a
+1 m cube of 1,000,000 fluid particles at 0.01 m in a 3 x 1.5 x 1 m tank of
+566,742 boundary particles, h = 0.02, dt <= 2e-4 (CFL), density tolerance 0.1%,
+divergence tolerance 1%.  A step is one substep of the reference's ``run_step``
+(``cfl_condition`` + ``sph_step``, main.py:347-352) over the whole scene; the
+metric counts fluid particles only (SURVEY-defined particle-steps/s).
+
+Output: one JSON line on rank 0.  ``value`` is timed with CUDA events on the
+solver's stream around K substeps whose inputs are already on the GPU; ``e2e``
+times the same substeps through the public Python API with the fluid state
+copied from pinned host memory before each substep and positions / velocities
+and the step scalars copied back after it.  ``roofline`` takes the step phase
+with the largest share of the step time, its algorithmic bytes per launch
+(per-particle figures in the design doc) and its mean launch time measured here with
+CUDA events (``tsph_profile_phases``).  ``cpu_baseline`` times the C
+restatement of the reference (``oracle/sph_port.c``, FP32, OpenMP on every host
+core) on a bounded number of substeps of the same scene.
+
+Multi-GPU: the single scene does not shard (it has no independent parts), so
+N ranks run N independent replicas (weak scaling, no collective in the timed
+region); ``value`` sums the replicas.  ``--impl reference`` runs the reference's
+CPU algorithm (the C restatement: Taichi, which the reference compiles its
+kernels with, is not installed) on rank 0 only.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s"
+UNIT = "particle-steps/s"
+
+# Algorithmic bytes per particle per launch of each phase (FP32, 3D, s = 12 bytes
+# per vector): each particle's own fields read or written once; neighbour reads
+# are served on chip.  (fluid bytes, boundary bytes)
+ALGO_BYTES_3D = {
+    "grid": (24, 24),        # pos read, key write/read, slot write
+    "density": (24, 16),     # pos, mass -> density, alpha  |  pos, mass
+    "psi": (36, 16),         # pos, v_adv, mass, density -> psi_adv  |  pos, mass
+    "vel": (48, 16),         # pos, psi_adv, alpha, mass, v_adv r/w  |  pos, mass
+    "advect": (44, 0),       # pos, v, mass, density -> v_adv
+    "unsort": (52, 0),       # v_adv, pos, mass -> pos, v
+    "cfl": (12, 0),
+}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1
+    import torch.distributed as dist
+    import torch
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    dist.init_process_group(backend)
+    return dist, dist.get_rank(), ws
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", self.gpu_id],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _ncu_traffic(kernel):
+    """DRAM bytes per particle of one launch of `kernel`, from the committed ncu
+    summary ``profiles/ncu_traffic.txt`` (lines: kernel dram_bytes fluid bound)."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for ln in f:
+            t = ln.split()
+            if len(t) >= 4 and t[0] == kernel and not ln.startswith("#"):
+                return float(t[1]), int(t[2]), int(t[3])
+    return None
+
+
+def build_sim(n_side, device):
+    from tichi_sph_gb300 import sph_config, workloads
+    from tichi_sph_gb300.simulation import Simulation
+    cfg_d, scen_d = workloads.dambreak_3d(n_side)
+    cfg = sph_config.Config(cfg_d, scen_d)
+    sim = Simulation(cfg, device=device)
+    sim.init_scenario()
+    return cfg, sim
+
+
+def cpu_baseline(n_side, budget_s, max_steps):
+    """C restatement of the reference (FP32, OpenMP) on the same initial state."""
+    from oracle.port import PortSim
+    from tichi_sph_gb300 import sph_config, workloads
+    from tichi_sph_gb300.simulation import Simulation
+    cfg_d, scen_d = workloads.dambreak_3d(n_side)
+    cfg = sph_config.Config(cfg_d, scen_d)
+    sim = Simulation(cfg, device="cpu")
+    sim.init_scenario()
+    keys = ["pos", "vel", "volume_frac", "rest_volume", "mass", "rest_density"]
+    fa = {k: getattr(sim.fluid, k)[:sim.fluid.part_num[None]].numpy() for k in keys}
+    ba = {k: getattr(sim.bound, k)[:sim.bound.part_num[None]].numpy() for k in keys}
+    port = PortSim(cfg, fa, ba)
+    nf = sim.fluid.part_num[None]
+    t0 = time.perf_counter()
+    steps = 0
+    iters = []
+    while steps < max_steps:
+        st = port.substep()
+        iters.append((st["div_iter"], st["incom_iter"]))
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    thr = port.threads()
+    port.close()
+    return {"value": nf * steps / el, "unit": UNIT, "cores": thr, "kind": "port",
+            "sample": "%d substeps of the full scene from rest (%d fluid + %d boundary particles), %.1f s, "
+                      "C restatement of the reference kernels (oracle/sph_port.c), FP32" % (
+                          steps, nf, sim.bound.part_num[None], el),
+            "ms_per_step": el / steps * 1e3, "iters": iters}
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return 0
+    n_side = args.n_side
+    res = cpu_baseline(n_side, budget_s=args.ref_budget, max_steps=args.warmup + args.steps)
+    nf = n_side ** 3
+    line = {
+        "metric": METRIC, "value": res["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": len(res["iters"]), "warmup": 0, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "3D DFSPH dam break, %d fluid + 566742 boundary particles, h=0.02, "
+                               "dt<=2e-4, rho tol 0.1%%" % nf, "fluid_particles": nf},
+        "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "Taichi (the reference's kernel compiler) is not installed; the reference's kernel sequence "
+                "runs as its C restatement on the host cores",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-side", type=int, default=100)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--ref-budget", type=float, default=150.0)
+    ap.add_argument("--hostloop", action="store_true",
+                    help="host-driven solver loops instead of the CUDA graph (kernels launched one by one, "
+                         "as profilers list them)")
+    ap.add_argument("--no-profile", action="store_true", help="skip the per-phase timing (roofline)")
+    ap.add_argument("--tpp", type=int, default=0, help="threads per particle (0: autotune after warm-up)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist, rank, ws = _dist()
+    if args.impl == "reference":
+        rc = run_reference(args, rank, ws)
+        if dist:
+            dist.destroy_process_group()
+        return rc
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg, sim = build_sim(args.n_side, dev)
+    solver = sim.solver
+    if args.hostloop:
+        solver.set_graph_mode(False)
+    nf, nb = sim.fluid.part_num[None], sim.bound.part_num[None]
+    stream = torch.cuda.current_stream(dev)
+
+    tune = None
+    if args.tpp:
+        solver.set_threads_per_particle(args.tpp)
+    for i in range(args.warmup):
+        solver.substep()
+        if i == 0 and not args.tpp:
+            tune = solver.autotune()
+    torch.cuda.synchronize(dev)
+    s0 = solver.stats()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        uuid = str(local)
+    clocks = ClockSampler(uuid)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        solver.substep()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    s1 = solver.stats()
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = nf * args.steps * ws / (ms / 1e3)
+    k_div = (s1["total_div_iter"] - s0["total_div_iter"]) / args.steps
+    k_inc = (s1["total_incom_iter"] - s0["total_incom_iter"]) / args.steps
+    launches = int(args.steps * s1["launches_per_step"] + s1["launches_per_iter"] *
+                   ((s1["total_div_iter"] - s0["total_div_iter"]) + (s1["total_incom_iter"] - s0["total_incom_iter"])))
+
+    # per-phase launch times (CUDA events on the solver's stream), for the roofline
+    if args.no_profile:
+        ph = {k: 1.0 for k in ("cfl", "grid", "density", "psi", "vel", "advect", "unsort")}
+    else:
+        ph = solver.profile_phases(reps=5)
+    per_step = {"cfl": 1, "grid": 1, "density": 1, "psi": k_div + k_inc, "vel": k_div + k_inc,
+                "advect": 1, "unsort": 1}
+    share = {k: ph[k] * per_step[k] for k in ph}
+    top = max(share, key=share.get)
+    fb, bb = ALGO_BYTES_3D[top]
+    algo_bytes = fb * nf + bb * nb
+    achieved = algo_bytes / (ph[top] / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    tr = _ncu_traffic(top)
+    traffic = None
+    if tr is not None:
+        dram, f0, b0 = tr
+        traffic = dram * (fb * nf + bb * nb) / max(fb * f0 + bb * b0, 1)
+    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": ph[top],
+                "phase_ms_per_launch": ph, "phase_share_of_step": {k: share[k] / sum(share.values()) for k in share}}
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        keys = ["pos", "vel", "mass", "rest_density", "rest_volume", "volume_frac"]
+        # the fluid state lives in pinned host memory and round-trips every substep
+        host_in = {k: getattr(sim.fluid, k)[:nf].detach().to("cpu").pin_memory() for k in keys}
+        host_out = {k: host_in[k] for k in ("pos", "vel")}
+        h2d = sum(t.numel() * t.element_size() for t in host_in.values())
+        d2h = sum(t.numel() * t.element_size() for t in host_out.values()) + 8 * 5
+        barrier()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        e2 = torch.cuda.Event(enable_timing=True)
+        e3 = torch.cuda.Event(enable_timing=True)
+        e2.record(stream)
+        for _ in range(args.steps):
+            for k, t in host_in.items():
+                getattr(sim.fluid, k)[:nf].copy_(t, non_blocking=True)
+            solver.substep()
+            for k, t in host_out.items():
+                t.copy_(getattr(sim.fluid, k)[:nf], non_blocking=True)
+            solver.stats()  # the step's scalars to the host (synchronises)
+        e3.record(stream)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        barrier()
+        ems = e2.elapsed_time(e3)
+        if dist:
+            t = torch.tensor([ems], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        e2e = {"value": nf * args.steps * ws / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": ems / args.steps, "host_wall_s": wall}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(args.n_side, budget_s=args.cpu_budget, max_steps=20)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "3D DFSPH dam break, %d fluid + %d boundary particles, h=0.02, dt<=2e-4 (CFL), "
+                                   "rho tol 0.1%%, div tol 1%%, from rest" % (nf, nb),
+                       "fluid_particles": nf, "boundary_particles": nb, "parallelism": "replicas" if ws > 1 else "single",
+                       "mean_div_iter": k_div, "mean_incom_iter": k_inc,
+                       "max_density_error": s1["max_dens_compression"],
+                       "l2": "inputs larger than L2 (per-step state ~400 MB > 129 MB)",
+                       "threads_per_particle": solver.tpp, "autotune_ms": tune,
+                       "graph": "host-driven solver loops" if args.hostloop else
+                       "one CUDA graph per substep, device-side while nodes"},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

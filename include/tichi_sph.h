@@ -105,7 +105,28 @@ typedef struct tsph_stats {
     int32_t fluid_in_grid;
     int32_t bound_in_grid;
     int32_t steps;
+    /* cumulative over all steps of this context */
+    int64_t total_div_iter;
+    int64_t total_incom_iter;
+    int64_t total_fbm_passes;
+    double max_dens_compression;   /* largest compression left by a density solve */
+    int32_t launches_per_step;     /* kernels per step outside the solver / pass loops */
+    int32_t launches_per_iter;     /* kernels per solver iteration */
+    int32_t launches_per_pass;     /* kernels per volume-fraction pass */
+    int32_t pad;
 } tsph_stats;
+
+/* Phases timed by tsph_profile_phases, in output order. */
+enum {
+    TSPH_PH_CFL = 0,        /* cfl_condition */
+    TSPH_PH_GRID = 1,       /* cell grid build + gather into sorted order */
+    TSPH_PH_DENSITY = 2,    /* density / alpha sweeps (fluid, boundary) */
+    TSPH_PH_PSI = 3,        /* Jacobi sweep A: psi_adv and its reduction */
+    TSPH_PH_VEL = 4,        /* Jacobi sweep B: v_adv update + loop test */
+    TSPH_PH_ADVECT = 5,     /* viscosity, surface tension, v_adv predict */
+    TSPH_PH_UNSORT = 6,     /* update + write-back in caller order */
+    TSPH_PH_COUNT = 7
+};
 
 typedef struct tsph_ctx tsph_ctx;
 
@@ -120,6 +141,11 @@ int tsph_destroy(tsph_ctx *ctx);
  * device-side while nodes (default), 0 = host-driven loops that read the
  * convergence value every iteration like main.py:201,222. */
 int tsph_set_graph_mode(tsph_ctx *ctx, int use_graph);
+
+/* Threads per particle of the neighbour-list sweeps (1, 2, 4 or 8; default 1).
+ * A tuning knob with no counterpart in the reference: results are the same up to
+ * FP32 summation order, and deterministic for a given setting. */
+int tsph_set_threads_per_particle(tsph_ctx *ctx, int threads_per_particle);
 
 /* cfl_condition(fluid), sph.py:41-47: dt on the device.  Also adds dt to the
  * device clock, as run_step does on the host (main.py:348-349). */
@@ -148,6 +174,13 @@ int tsph_set_state(tsph_ctx *ctx, double time_count, float dt, double compressio
 int tsph_neighbor_stats(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound,
                         int32_t *fluid_counts, uint64_t *fluid_hash,
                         int32_t *bound_counts, uint64_t *bound_hash, void *stream);
+
+/* Measurement: runs each phase of a step `reps` times back to back on `stream`
+ * and writes its mean duration per launch in milliseconds (CUDA events on that
+ * stream) to ms_out[TSPH_PH_COUNT].  The phases leave the particle state as one
+ * step would (positions advance once); synchronises. */
+int tsph_profile_phases(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, int reps,
+                        float *ms_out, void *stream);
 
 /* Library version string. */
 const char *tsph_version(void);

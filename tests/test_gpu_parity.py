@@ -215,3 +215,44 @@ def test_neighbor_sets_bit_exact(scene):
         np.testing.assert_array_equal(cnt_gpu[keep, 1], cb[keep])
         np.testing.assert_array_equal(hash_gpu[keep].view(np.uint64), (hf + hb)[keep])
     solver.close()
+
+
+@pytest.mark.parametrize("tpp", [1, 2, 8])
+@pytest.mark.parametrize("scene", ["dfsph3d", "vfsph2d", "edge2d"])
+def test_threads_per_particle_settings(scene, tpp):
+    """Every threads-per-particle setting of the list sweeps meets the one-step bar."""
+    _need_cuda()
+    init, gold = G.load(scene)
+    fa, ba = G.init_arrays(init, "fluid"), G.init_arrays(init, "bound")
+    cfg, fl, bd, solver = make_gpu(scene, fa, ba)
+    solver.set_threads_per_particle(tpp)
+    p, ofl, obd = make_oracle(scene, fa, ba)
+    solver.substep()
+    gs = solver.stats()
+    st = O.run_substep(ofl, obd, p, O.Stats(), fbm=scene in G.FBM_SCENES)
+    assert (gs["div_iter"], gs["incom_iter"]) == (st.div_iter, st.incom_iter)
+    dens = float(np.abs(ofl.sph_density).max(initial=0.0))
+    fdt = st.dt if scene in G.FBM_SCENES else None
+    compare(scene, "tpp%d" % tpp, fl, ofl, _fluid_fields(scene, p), dens_scale=dens, fbm_dt=fdt)
+    solver.close()
+
+
+@pytest.mark.parametrize("scene", ["dfsph3d", "vfsph2d"])
+def test_bitwise_deterministic(scene):
+    """Same inputs, same settings: bit-identical state after several substeps
+    (ordered cell slots, fixed neighbour order, fixed-order FP64 reductions)."""
+    _need_cuda()
+    init, gold = G.load(scene)
+    fa, ba = G.init_arrays(init, "fluid"), G.init_arrays(init, "bound")
+    outs = []
+    for _ in range(2):
+        cfg, fl, bd, solver = make_gpu(scene, fa, ba)
+        for _ in range(3):
+            solver.substep()
+        st = solver.stats()
+        outs.append((fl.pos.cpu().numpy().copy(), fl.vel.cpu().numpy().copy(),
+                     fl.volume_frac.cpu().numpy().copy(), st["compression"], st["kinetic_energy"]))
+        solver.close()
+    a, b = outs
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(np.asarray(x), np.asarray(y))

@@ -53,7 +53,13 @@ class Stats(C.Structure):
         ("kinetic_energy", C.c_double), ("potential_energy", C.c_double),
         ("div_iter", _i32), ("incom_iter", _i32), ("fbm_passes", _i32), ("general_flag", _i32),
         ("status", _i32), ("fluid_in_grid", _i32), ("bound_in_grid", _i32), ("steps", _i32),
+        ("total_div_iter", _i64), ("total_incom_iter", _i64), ("total_fbm_passes", _i64),
+        ("max_dens_compression", C.c_double),
+        ("launches_per_step", _i32), ("launches_per_iter", _i32), ("launches_per_pass", _i32), ("pad", _i32),
     ]
+
+
+PHASES = ["cfl", "grid", "density", "psi", "vel", "advect", "unsort"]
 
 
 class Ctx(C.Structure):
@@ -67,6 +73,7 @@ SIGNATURES = {
     "tsph_create": (C.c_int, [C.POINTER(Params), _i64, _i64, C.POINTER(CtxP)]),
     "tsph_destroy": (C.c_int, [CtxP]),
     "tsph_set_graph_mode": (C.c_int, [CtxP, C.c_int]),
+    "tsph_set_threads_per_particle": (C.c_int, [CtxP, C.c_int]),
     "tsph_cfl_condition": (C.c_int, [CtxP, C.POINTER(Set), C.c_void_p]),
     "tsph_sph_step": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p]),
     "tsph_substep": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p]),
@@ -74,6 +81,7 @@ SIGNATURES = {
     "tsph_set_state": (C.c_int, [CtxP, C.c_double, C.c_float, C.c_double, C.c_void_p]),
     "tsph_neighbor_stats": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), _ip, C.POINTER(C.c_uint64),
                                       _ip, C.POINTER(C.c_uint64), C.c_void_p]),
+    "tsph_profile_phases": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_int, _fp, C.c_void_p]),
     "tsph_version": (C.c_char_p, []),
     "tsph_last_error": (C.c_char_p, []),
 }

@@ -89,6 +89,7 @@ __global__ void k_solve_empty(KConst k, DevStep *ds, DevPersist *dp, int kind) {
 int solve(tsph_ctx &c, int64_t nf, int kind, cudaStream_t st, bool graph) {
     if (nf <= 0) {
         k_solve_empty<<<1, 1, 0, st>>>(c.k, c.ds, c.dp, kind);
+        c.launches += 1;
         return TSPH_OK;
     }
     if (!graph) {
@@ -97,7 +98,9 @@ int solve(tsph_ctx &c, int64_t nf, int kind, cudaStream_t st, bool graph) {
             TSPH_CK(cudaMemcpyAsync(&c.host_ds->cond, &c.ds->cond, sizeof(int), cudaMemcpyDeviceToHost, st));
             TSPH_CK(cudaStreamSynchronize(st));
             if (!c.host_ds->cond) break;
+            const int save = c.launches;  // loop-body launches are counted per iteration
             launch_solve_iter(c, nf, kind, 0, 0, st);
+            c.launches = save;
         }
         return TSPH_OK;
     }
@@ -121,7 +124,9 @@ int solve(tsph_ctx &c, int64_t nf, int kind, cudaStream_t st, bool graph) {
     cudaGraph_t body = np.conditional.phGraph_out[0];
     cudaStream_t bs = extra(&c)->body_stream;
     TSPH_CK(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const int save = c.launches;
     launch_solve_iter(c, nf, kind, h, 1, bs);
+    c.launches = save;
     cudaGraph_t tmp;
     TSPH_CK(cudaStreamEndCapture(bs, &tmp));
     return TSPH_OK;
@@ -134,7 +139,9 @@ int fbm_loop(tsph_ctx &c, int64_t nf, cudaStream_t st, bool graph) {
             TSPH_CK(cudaMemcpyAsync(&c.host_ds->fbm_cond, &c.ds->fbm_cond, sizeof(int), cudaMemcpyDeviceToHost, st));
             TSPH_CK(cudaStreamSynchronize(st));
             if (!c.host_ds->fbm_cond) break;
+            const int save = c.launches;
             launch_fbm_pass(c, nf, 0, 0, st);
+            c.launches = save;
         }
         return TSPH_OK;
     }
@@ -158,7 +165,9 @@ int fbm_loop(tsph_ctx &c, int64_t nf, cudaStream_t st, bool graph) {
     cudaGraph_t body = np.conditional.phGraph_out[0];
     cudaStream_t bs = extra(&c)->body_stream;
     TSPH_CK(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const int save = c.launches;
     launch_fbm_pass(c, nf, h, 1, bs);
+    c.launches = save;
     cudaGraph_t tmp;
     TSPH_CK(cudaStreamEndCapture(bs, &tmp));
     return TSPH_OK;
@@ -166,6 +175,7 @@ int fbm_loop(tsph_ctx &c, int64_t nf, cudaStream_t st, bool graph) {
 
 // Enqueues one step (optionally preceded by cfl_condition) on `st`.
 int enqueue_step(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st, bool with_cfl, bool graph) {
+    c.launches = 0;
     launch_step_begin(c, st);
     if (with_cfl) launch_cfl(c, f, st);
     launch_grid_build(c, f, b, st);
@@ -180,6 +190,7 @@ int enqueue_step(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t
         if (rc) return rc;
     }
     launch_unsort(c, f, b, st);
+    c.launches_per_step = c.launches;
     return TSPH_OK;
 }
 
@@ -339,6 +350,9 @@ int tsph_create(const tsph_params *p, int64_t capf, int64_t capb, tsph_ctx **out
     F.facc = A.get<float4>(capf);
     F.zeta = A.get<float>(capf);
     F.flagpass = A.get<int>(capf);
+    k.nbr_max = p->dim == 3 ? 64 : 32;  // a multiple of 4 (blocked layout)
+    F.nbr = A.get<int>((int64_t)k.nbr_max * capf);
+    F.nbr_cnt = A.get<unsigned int>(capf);
     BoundBuf &B = c.B;
     B.cap = capb;
     B.count = A.get<int>(nn);
@@ -356,7 +370,7 @@ int tsph_create(const tsph_params *p, int64_t capf, int64_t capb, tsph_ctx **out
     B.a2 = A.get<float>(capb);
     B.alpha = A.get<float>(capb);
     const int64_t nmax = capf > capb ? capf : capb;
-    c.S.partials_len = 2 * (int64_t)blocks_for(nmax) + 64;
+    c.S.partials_len = 8 * (int64_t)blocks_for(nmax) + 64;  // up to 8 threads per particle
     c.S.partials = A.get<double>(c.S.partials_len);
     const int64_t nscan = (nn + 4095) / 4096 + 1;
     c.S.scan_len = 2 * nscan;
@@ -379,6 +393,7 @@ int tsph_create(const tsph_params *p, int64_t capf, int64_t capb, tsph_ctx **out
         return rc;
     }
     c.use_graph = 1;
+    c.tpp = 1;
     *out = &c;
     return TSPH_OK;
 }
@@ -399,6 +414,17 @@ int tsph_destroy(tsph_ctx *c) {
 int tsph_set_graph_mode(tsph_ctx *c, int use_graph) {
     if (!c) return fail(TSPH_ERR_INVALID, "null ctx");
     c->use_graph = use_graph ? 1 : 0;
+    return TSPH_OK;
+}
+
+int tsph_set_threads_per_particle(tsph_ctx *c, int tpp) {
+    if (!c) return fail(TSPH_ERR_INVALID, "null ctx");
+    if (tpp != 1 && tpp != 2 && tpp != 4 && tpp != 8) return fail(TSPH_ERR_INVALID, "threads per particle must be 1, 2, 4 or 8");
+    if (tpp != c->tpp && c->exec) {
+        cudaGraphExecDestroy(c->exec);
+        c->exec = nullptr;
+    }
+    c->tpp = tpp;
     return TSPH_OK;
 }
 
@@ -439,6 +465,60 @@ int tsph_read_stats(tsph_ctx *c, tsph_stats *out, void *stream) {
     out->fluid_in_grid = -1;
     out->bound_in_grid = -1;
     out->steps = c->stepped;
+    out->total_div_iter = d.total_div_iter;
+    out->total_incom_iter = d.total_incom_iter;
+    out->total_fbm_passes = d.total_fbm_passes;
+    out->max_dens_compression = d.max_dens_compression;
+    out->launches_per_step = c->launches_per_step;
+    out->launches_per_iter = 2;
+    out->launches_per_pass = 1;
+    return TSPH_OK;
+}
+
+int tsph_profile_phases(tsph_ctx *c, const tsph_set *f, const tsph_set *b, int reps, float *ms_out, void *stream) {
+    if (!c || !f || !b || !ms_out || reps < 1) return fail(TSPH_ERR_INVALID, "bad argument");
+    if (f->n > c->F.cap || b->n > c->B.cap) return fail(TSPH_ERR_CAPACITY, "part_num above capacity");
+    cudaStream_t st = (cudaStream_t)stream;
+    // keep the persistent scalars (clock, counters) as they were
+    TSPH_CK(cudaMemcpyAsync(c->host_dp, c->dp, sizeof(DevPersist), cudaMemcpyDeviceToHost, st));
+    TSPH_CK(cudaStreamSynchronize(st));
+    const DevPersist saved = *c->host_dp;
+    cudaEvent_t e0, e1;
+    TSPH_CK(cudaEventCreate(&e0));
+    TSPH_CK(cudaEventCreate(&e1));
+    const int64_t nf = f->n, nb = b->n;
+    for (int ph = 0; ph < TSPH_PH_COUNT; ++ph) {
+        // state every phase expects: a fresh step through the density sweep
+        launch_step_begin(*c, st);
+        launch_cfl(*c, *f, st);
+        launch_grid_build(*c, *f, *b, st);
+        launch_density(*c, nf, nb, st);
+        launch_solve_begin(*c, kSolveDiv, 0, 0, st);
+        if (nf > 0) launch_psi(*c, nf, st);
+        TSPH_CK(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps; ++r) {
+            switch (ph) {
+                case TSPH_PH_CFL: launch_cfl(*c, *f, st); break;
+                case TSPH_PH_GRID: launch_grid_build(*c, *f, *b, st); break;
+                case TSPH_PH_DENSITY: launch_density(*c, nf, nb, st); break;
+                case TSPH_PH_PSI: if (nf > 0) launch_psi(*c, nf, st); break;
+                case TSPH_PH_VEL: if (nf > 0) launch_vel(*c, nf, kSolveDiv, 0, 0, st); break;
+                case TSPH_PH_ADVECT: launch_advect(*c, nf, st); break;
+                case TSPH_PH_UNSORT: launch_unsort(*c, *f, *b, st); break;
+            }
+        }
+        TSPH_CK(cudaEventRecord(e1, st));
+        TSPH_CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        TSPH_CK(cudaEventElapsedTime(&ms, e0, e1));
+        ms_out[ph] = ms / reps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *c->host_dp = saved;
+    TSPH_CK(cudaMemcpyAsync(c->dp, c->host_dp, sizeof(DevPersist), cudaMemcpyHostToDevice, st));
+    TSPH_CK(cudaStreamSynchronize(st));
+    TSPH_CK(cudaGetLastError());
     return TSPH_OK;
 }
 

@@ -29,6 +29,8 @@ struct DevPersist {
     double compression;  // carried into the next divergence-loop test (main.py:201)
     float dt;
     int32_t steps;
+    long long total_div_iter, total_incom_iter, total_fbm_passes;
+    double max_dens_compression;
 };
 
 // Scalars of one step; zeroed by a memset at the start of every step.
@@ -44,6 +46,7 @@ struct DevStep {
     int32_t gflag_out;          // general_flag after the last volume-fraction pass
     unsigned int ticket[8];
     double kinetic_energy, potential_energy;
+    double psi_sum;             // sum of psi_adv / psi0 of the last Jacobi sweep A
 };
 
 // Launch-time constants of one context (passed by value: lands in the constant bank).
@@ -60,7 +63,17 @@ struct KConst {
     int cs, iter_min, iter_max, fbm_max_passes;
     float div_tol, comp_tol;
     float c_coh;                      // 32 / (pi h^3), cohesion normaliser
+    int nbr_max;                      // neighbour-list slots per fluid particle
 };
+
+// nbr_cnt value of a particle whose neighbours did not fit the list: its sweeps
+// scan the template cells instead.
+constexpr unsigned int kNbrOverflow = 0xffffffffu;
+
+// Position of neighbour t of sorted particle s in the blocked neighbour list.
+__host__ __device__ __forceinline__ int64_t nbr_index(int t, int64_t s, int64_t cap) {
+    return (((int64_t)(t >> 2)) * cap + s) * 4 + (t & 3);
+}
 
 struct FluidBuf {
     int64_t cap;
@@ -81,6 +94,13 @@ struct FluidBuf {
     float4 *facc;            // acce (fbm_acce)
     float *zeta;
     int *flagpass;           // 0 = unflagged, else the FBM pass that flagged it
+    // Neighbours with 0 < r < h, recorded by the density sweep in candidate order:
+    // first the fluid neighbours of sorted particle s, then its boundary ones, in
+    // blocks of four: entry t sits at nbr[nbr_index(t, s, cap)], so block t / 4 of
+    // 32 consecutive particles is one 512-byte run (one int4 per particle).
+    // nbr_cnt[s] packs the two counts (fluid | boundary << 16) or is kNbrOverflow.
+    int *nbr;
+    unsigned int *nbr_cnt;
 };
 
 struct BoundBuf {
@@ -206,6 +226,144 @@ __device__ __forceinline__ double sum_partials(const double *partials, int n, do
     double v = 0.0;
     for (int i = threadIdx.x; i < n; i += BS) v += __ldcg(partials + i);
     return block_sum<BS>(v, sh);
+}
+
+// Per-block FP64 sum without a block-wide barrier at the end (warps finish at
+// different times in the neighbour sweeps): each warp leaves its sum in shared
+// memory, the last warp to arrive adds the block's warp sums in warp order and
+// returns true with the result in `out` (lane 0).  `arrived` must be zeroed
+// before any warp can arrive (a barrier at kernel start).
+template <int BS>
+__device__ __forceinline__ bool block_sum_last_warp(double v, double *sh, unsigned int *arrived, double &out) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned int old = 0;
+    if (lane == 0) {
+        sh[w] = v;
+        __threadfence_block();
+        old = atomicAdd(arrived, 1u);
+    }
+    old = __shfl_sync(0xffffffffu, old, 0);
+    if (old != BS / 32 - 1) return false;
+    __threadfence_block();
+    double s = 0.0;
+    if (lane == 0)
+        for (int i = 0; i < BS / 32; ++i) s += ((volatile double *)sh)[i];
+    out = s;
+    return true;
+}
+
+// Grid-wide version for one warp: true (in all its lanes) for the warp that
+// arrives last among `total` arriving warps.
+__device__ __forceinline__ bool last_warp_done(unsigned int *ticket, unsigned int total) {
+    const int lane = threadIdx.x & 31;
+    unsigned int t = 0;
+    if (lane == 0) {
+        __threadfence();
+        t = atomicAdd(ticket, 1u);
+    }
+    t = __shfl_sync(0xffffffffu, t, 0);
+    const bool last = (t == total - 1);
+    if (last) __threadfence();
+    return last;
+}
+
+// Like visit_candidates, but lane q of a TPP-lane particle group visits only the
+// candidates j = beg + q, beg + q + TPP, ... of every row.
+template <int DIM, int TPP, class F>
+__device__ __forceinline__ void visit_candidates_strided(const int *__restrict__ start, const KConst &k,
+                                                         long long code, int q, F &&f) {
+    const int R = k.R;
+    const int zr = (DIM == 3) ? R : 0;
+    for (int dz = -zr; dz <= zr; ++dz) {
+        for (int dy = -R; dy <= R; ++dy) {
+            long long rc = code + dy * k.nx + dz * k.nxny;
+            long long lo = rc - R, hi = rc + R;
+            if (lo < 1) lo = 1;
+            if (hi > k.node_num - 1) hi = k.node_num - 1;
+            if (lo > hi) continue;
+            const int beg = __ldg(start + lo);
+            const int end = __ldg(start + hi + 1);
+            for (int j = beg + q; j < end; j += TPP) f(j);
+        }
+    }
+}
+
+// Lane layout of a sweep with TPP threads per particle: a warp serves 32 / TPP
+// consecutive particles; lane = q * (32 / TPP) + p handles particle p of the warp
+// and every TPP-th four-entry block of its neighbour list starting at block q, so
+// lanes with the same q read one contiguous 16 * 32 / TPP-byte run of the list.
+template <int TPP>
+struct Lanes {
+    static constexpr int PPW = 32 / TPP;  // particles per warp
+    int q, p;
+    int64_t s;
+    __device__ __forceinline__ Lanes() {
+        const int lane = threadIdx.x & 31;
+        q = lane / PPW;
+        p = lane % PPW;
+        const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+        s = warp * PPW + p;
+    }
+    // sum over the TPP lanes of the particle (fixed xor tree: deterministic)
+    __device__ __forceinline__ float sum(float v) const {
+#pragma unroll
+        for (int o = PPW; o < 32; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return v;
+    }
+};
+
+// Walks the blocked neighbour list of sorted particle s for lane q of a TPP-lane
+// group: blocks b = q, q + TPP, ... of four entries; entries t < nfl are fluid
+// neighbours (ff), nfl <= t < ntot boundary ones (fb).  The next block's int4 is
+// loaded before the current block is processed, and the four callbacks of a
+// block only accumulate into registers, so their gathers can all be in flight
+// together.
+template <int TPP, class FF, class FB>
+__device__ __forceinline__ void walk_blocks(const int *__restrict__ nbr, int64_t s, int64_t cap, int q,
+                                            int nfl, int ntot, FF &&ff, FB &&fb) {
+    const int4 *L4 = reinterpret_cast<const int4 *>(nbr) + s;
+    const int nblk = (ntot + 3) >> 2;
+    int b = q;
+    if (b >= nblk) return;
+    int4 cur = __ldg(L4 + (int64_t)b * cap);
+    while (b < nblk) {
+        const int bn = b + TPP;
+        int4 nxt = cur;
+        if (bn < nblk) nxt = __ldg(L4 + (int64_t)bn * cap);
+        const int t0 = b << 2;
+        const int jj[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int t = t0 + e;
+            if (t < nfl) ff(jj[e]);
+            else if (t < ntot) fb(jj[e]);
+        }
+        cur = nxt;
+        b = bn;
+    }
+}
+
+// Neighbours of sorted fluid particle s for lane q of a TPP-lane particle group:
+// the blocked list, or -- for a particle whose list overflowed -- the strided
+// candidate scan of the template cells.  Both visit the pairs the density sweep
+// selected; the callbacks keep their own 0 < r < h test, which is what selects
+// the pairs on the scanning path.
+template <int DIM, bool BOUND, int TPP, class FF, class FB>
+__device__ __forceinline__ void for_each_neighbor_tpp(const KConst &k, const FluidBuf &F, const BoundBuf &B,
+                                                      int64_t s, int q, float4 pi, FF &&ff, FB &&fb) {
+    const unsigned int pc = F.nbr_cnt[s];
+    if (pc != kNbrOverflow) {
+        const int nfl = (int)(pc & 0xffffu), nbo = (int)(pc >> 16);
+        walk_blocks<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl, ff, fb);
+    } else {
+        bool ok;
+        const long long code = cell_code<DIM>(pi, k, ok);
+        if (ok) {
+            visit_candidates_strided<DIM, TPP>(F.start, k, code, q, ff);
+            if (BOUND) visit_candidates_strided<DIM, TPP>(B.start, k, code, q, fb);
+        }
+    }
 }
 
 inline int blocks_for(int64_t n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }

@@ -21,6 +21,9 @@ struct tsph_ctx {
     cudaGraphExec_t exec;
     unsigned long long graph_key[4];
     int graph_substep;         // whether the cached graph includes cfl_condition
+    int launches;              // kernel launches enqueued (counted by the launchers)
+    int launches_per_step;     // top-level kernels of the last enqueued step
+    int tpp;                   // threads per particle of the list sweeps (1, 2, 4, 8)
 };
 
 namespace tsph {
@@ -41,6 +44,9 @@ void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int
                         cudaStream_t st);
 void launch_solve_iter(tsph_ctx &c, int64_t nf, int kind, cudaGraphConditionalHandle h,
                        int use_cond, cudaStream_t st);
+void launch_psi(tsph_ctx &c, int64_t nf, cudaStream_t st);
+void launch_vel(tsph_ctx &c, int64_t nf, int kind, cudaGraphConditionalHandle h, int use_cond,
+                cudaStream_t st);
 void launch_advect(tsph_ctx &c, int64_t nf, cudaStream_t st);
 
 // fbm.cu

@@ -93,10 +93,8 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, int64
 #pragma unroll
             for (int q = 0; q < P; ++q) ui[q] = F.drift[q * F.cap + s];
             const float cc = k.fbm_c * dt, cd = dt * k.fbm_D, eps = 0.01f * k.h2;
-            bool ok;
-            const long long code = cell_code<DIM>(pi, k, ok);
-            if (ok) {
-                visit_candidates<DIM>(F.start, k, code, [&](int j) {
+            for_each_neighbor_tpp<DIM, false, 1>(k, F, BoundBuf{}, s, 0, pi,
+                [&](int j) {
                     const float4 pj = F.pos[j];
                     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                     const float r2 = dx * dx + dy * dy + dz * dz;
@@ -118,8 +116,8 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, int64
                         tmp[q] -= cc * Vj * (fx * gx + fy * gy + fz * gz);
                         tmp[q] += (vfi[q] - vfj) * dif;
                     }
-                });
-            }
+                },
+                [&](int) {});
         }
         bool neg = false;
 #pragma unroll
@@ -179,11 +177,13 @@ static void fbm_dispatch(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, 
 
 void launch_fbm_begin(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
     cudaMemsetAsync(c.F.flagpass, 0, sizeof(int) * (nf > 0 ? nf : 1), st);
+    c.launches += 1 + (nf > 0);
     if (nf > 0) fbm_dispatch(c, nf, 0, 0, st, true);
     k_fbm_begin<<<1, 1, 0, st>>>(c.ds, h, use_cond);
 }
 
 void launch_fbm_pass(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+    c.launches += 1;
     fbm_dispatch(c, nf, h, use_cond, st, false);
 }
 

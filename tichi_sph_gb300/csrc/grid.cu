@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, B
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_unsort_fluid(KConst k, tsph_set U, FluidBuf F,
                                                          const int *__restrict__ bstart, DevStep *ds,
-                                                         const DevPersist *dp, double *partials,
+                                                         DevPersist *dp, double *partials,
                                                          int fbm, int st_on) {
     __shared__ double sh[kBlock / 32];
     const int64_t pid = blockIdx.x * (int64_t)kBlock + threadIdx.x;
@@ -355,6 +355,10 @@ __global__ void __launch_bounds__(kBlock) k_unsort_fluid(KConst k, tsph_set U, F
             ds->kinetic_energy = a;
             ds->potential_energy = b;
             ds->ticket[1] = 0;
+            dp->total_div_iter += ds->div_iter;
+            dp->total_incom_iter += ds->incom_iter;
+            dp->total_fbm_passes += ds->fbm_passes;
+            dp->max_dens_compression = fmax(dp->max_dens_compression, dp->compression);
         }
     }
 }
@@ -429,6 +433,7 @@ void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st) {
     int nb = blocks_for(f.n);
     if (nb < 1) nb = 1;
     if (nb > 4 * 152) nb = 4 * 152;
+    c.launches += 1;
     if (c.k.dim == 3) k_cfl<3><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n, c.ds, c.dp);
     else k_cfl<2><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n, c.ds, c.dp);
 }
@@ -437,6 +442,7 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     const int64_t nn = c.k.node_num;
     cudaMemsetAsync(c.F.count, 0, sizeof(int) * nn, st);
     cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, st);
+    c.launches += (f.n > 0) + (b.n > 0) + 3 + 1 + (f.n > 0) + (b.n > 0) + ((f.n > 0 || b.n > 0) ? 1 : 0);
     if (f.n > 0) {
         if (c.k.dim == 3) k_encode<3><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, c.F.count, c.F.slot, &c.ds->f_tail, &c.ds->status);
         else k_encode<2><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, c.F.count, c.F.slot, &c.ds->f_tail, &c.ds->status);
@@ -486,6 +492,7 @@ void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream
     const int st_on = c.k.gamma != 0.f ? 1 : 0;
     int nb = blocks_for(f.n);
     if (nb < 1) nb = 1;
+    c.launches += 1 + (b.n > 0);
     if (c.k.dim == 3) k_unsort_fluid<3><<<nb, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.ds, c.dp, c.S.partials, fbm, st_on);
     else k_unsort_fluid<2><<<nb, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.ds, c.dp, c.S.partials, fbm, st_on);
     if (b.n > 0) {

@@ -41,10 +41,29 @@ class Solver:
                                 _native.C.byref(ctx)), "tsph_create")
         self.ctx = ctx
         self.set_graph_mode(use_graph)
+        self.tpp = 1
         self._stats = _native.Stats()
 
     def set_graph_mode(self, use_graph):
         check(self._lib.tsph_set_graph_mode(self.ctx, 1 if use_graph else 0), "tsph_set_graph_mode")
+
+    def set_threads_per_particle(self, tpp):
+        """Lanes per particle of the neighbour-list sweeps (1, 2, 4, 8)."""
+        check(self._lib.tsph_set_threads_per_particle(self.ctx, int(tpp)), "tsph_set_threads_per_particle")
+        self.tpp = int(tpp)
+
+    def autotune(self, candidates=(1, 2, 4, 8), reps=5):
+        """Times the neighbour-list sweeps (Jacobi pair + advection) for each
+        threads-per-particle setting on the current state and keeps the fastest.
+        Returns {tpp: ms per Jacobi iteration + advection}."""
+        res = {}
+        for t in candidates:
+            self.set_threads_per_particle(t)
+            ph = self.profile_phases(reps=reps)
+            res[t] = ph["psi"] + ph["vel"] + ph["advect"]
+        best = min(res, key=res.get)
+        self.set_threads_per_particle(best)
+        return res
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -100,6 +119,17 @@ class Solver:
         self.fluid.statistics_gravity_potential_energy[None] = s.potential_energy
         self.fluid.general_flag[None] = s.general_flag
         return {k: getattr(s, k) for k, _ in _native.Stats._fields_}
+
+    def profile_phases(self, reps=10):
+        """Mean milliseconds per launch of each step phase (CUDA events on the
+        current stream); see ``tsph_profile_phases``."""
+        out = (_native.C.c_float * len(_native.PHASES))()
+        f, b = self._sets()
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_profile_phases(self.ctx, f, b, int(reps), out,
+                                                _native.C.c_void_p(_stream_handle(self.device))),
+                  "tsph_profile_phases")
+        return dict(zip(_native.PHASES, [float(v) for v in out]))
 
     def neighbor_stats(self):
         """Per-particle neighbour counts (fluid, boundary) and set hashes."""

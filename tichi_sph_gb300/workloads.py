@@ -1,0 +1,68 @@
+"""Benchmark scenes written in the reference's config / scenario JSON schema.
+
+Seeded synthetic stand-ins for the benchmark configurations (the reference
+publishes none): lattice blocks and boxes emitted by the reference's own emitter
+rules (``sph_obj.py:102-163``).
+
+* :func:`dambreak_2d` -- 2D single-phase DFSPH dam break: fluid 1.0 x 2.0 m at
+  0.02 m (50 x 100 = 5,000 particles) in a 4 x 4 m box with 3 boundary layers,
+  rest density 1000, gravity -9.81, viscosity 0.01, dt 1e-3 (``solver_cs`` 20:
+  dt = part_size / cs, CFL always on), tolerances 0.1% / 1%.
+* :func:`dambreak_3d` -- 3D single-phase DFSPH dam break: a 1 m cube at 0.01 m
+  (100^3 = 1,000,000 particles) in the x-min corner of a 3 x 1.5 x 1 m tank
+  (x, y up, z) with 3 boundary layers (566,742 particles), h = 0.02, rest density
+  1000, viscosity 0.01, ``solver_cs`` 50 so dt <= 2e-4 with CFL factor 0.5,
+  tolerances 0.1% / 1%.
+"""
+
+
+def _config(solver="DFSPH", cs=50, div_tol=1e-2, comp_tol=1e-3, gamma=0.0, fbm_c=0.0, fbm_d=0.0):
+    return {
+        "arch": "gpu", "device_memory_GB": 6,
+        "solver_type": solver, "solver_wc_gamma": 7,
+        "solver_divergence_threshold": div_tol, "solver_compression_threshold": comp_tol,
+        "solver_iter_threshold_min": 2, "solver_iter_threshold_max": 100,
+        "solver_if_cfl": True, "solver_cs": cs, "solver_cfl_factor": 0.5,
+        "solver_neighb_range": 1, "solver_neighb_grid_size_TO_global_part_size": 2,
+        "solver_fbm_diffusion_term": fbm_d, "solver_fbm_convection_term": fbm_c,
+        "solver_surface_tension_gamma": gamma,
+        "gui_res": [1080, 1080], "gui_part_zoomer": 1.0, "gui_fps": 30,
+        "gui_canvas_bgcolor": [0.2, 0.2, 0.6], "gui_camera_pos": [6.0, 1.0, 0.0],
+        "gui_camera_lookat": [0.0, 0.0, 0.0],
+    }
+
+
+def _obj(kind, start, end, vf, vel, rf=1.0, layers=None):
+    o = {"type": kind, "vel": vel, "particle_relaxing_factor": rf, "start_pos": start, "end_pos": end,
+         "volume_frac": vf, "color": "0x6F7DBC"}
+    if layers is not None:
+        o["layers"] = layers
+    return o
+
+
+def dambreak_2d():
+    cfg = _config(cs=20)
+    scen = {
+        "sim_env": {"global_part_size": 0.02, "global_dynamic_viscosity": 0.01, "sim_dim": 2,
+                    "sim_space_lb": [-0.2, -0.2], "sim_space_rt": [4.2, 4.2], "gravity": [0, -9.81],
+                    "phase_num": 1, "phase_rest_density": [1000], "phase_color_hex": ["0x6F7DBC"]},
+        "fluid": {"max_part_num": 5000, "objs": [_obj("cube", [0.0, 0.0], [1.0, 2.0], [1], [0, 0])]},
+        "bound": {"max_part_num": 4000, "objs": [_obj("box", [-0.07, -0.07], [3.93, 3.93], [1], [0, 0], layers=3)]},
+    }
+    return cfg, scen
+
+
+def dambreak_3d(n_side=100, spacing=0.01):
+    """A cube of n_side^3 fluid particles; n_side = 100 is the 1M-particle case."""
+    L = n_side * spacing
+    cfg = _config(cs=50)
+    scen = {
+        "sim_env": {"global_part_size": spacing, "global_dynamic_viscosity": 0.01, "sim_dim": 3,
+                    "sim_space_lb": [-0.15, -0.15, -0.15], "sim_space_rt": [3.2, 2.0, 1.2],
+                    "gravity": [0, -9.81, 0], "phase_num": 1, "phase_rest_density": [1000],
+                    "phase_color_hex": ["0x6F7DBC"]},
+        "fluid": {"max_part_num": n_side ** 3, "objs": [_obj("cube", [0.0, 0.0, 0.0], [L, L, L], [1], [0, 0, 0])]},
+        "bound": {"max_part_num": 566742, "objs": [
+            _obj("box", [-0.035, -0.035, -0.035], [3.035, 1.535, 1.035], [1], [0, 0, 0], layers=3)]},
+    }
+    return cfg, scen
