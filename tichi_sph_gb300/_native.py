@@ -82,6 +82,8 @@ SIGNATURES = {
     "tsph_neighbor_stats": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), _ip, C.POINTER(C.c_uint64),
                                       _ip, C.POINTER(C.c_uint64), C.c_void_p]),
     "tsph_profile_phases": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_int, _fp, C.c_void_p]),
+    "tsph_fluid_density_noalloc": (C.c_int, [C.POINTER(Params), _fp, _fp, _fp, _i64, _fp, _fp, _fp, _i64,
+                                             _fp, _fp, _fp, C.c_void_p]),
     "tsph_version": (C.c_char_p, []),
     "tsph_last_error": (C.c_char_p, []),
 }

@@ -271,6 +271,15 @@ const char *tsph_version(void) { return "tichi_sph_gb300 0.1 (sm_103a)"; }
 
 const char *tsph_last_error(void) { return g_last_error; }
 
+}  // extern "C"
+
+namespace tsph {
+// Lets other translation units report through tsph_last_error.
+void set_last_error_text(const char *msg) { std::snprintf(g_last_error, sizeof(g_last_error), "%s", msg); }
+}  // namespace tsph
+
+extern "C" {
+
 int tsph_create(const tsph_params *p, int64_t capf, int64_t capb, tsph_ctx **out) {
     if (!p || !out) return fail(TSPH_ERR_INVALID, "null argument");
     *out = nullptr;
