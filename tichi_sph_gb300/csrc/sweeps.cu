@@ -19,8 +19,64 @@ namespace tsph {
 // SPH_clean_value + SPH_prepare_attr (f,f)(f,b) + SPH_prepare_alpha_1 (f,f)(f,b)
 // + SPH_prepare_alpha_2 (f,f) + SPH_prepare_alpha (sph.py:22-38, 50-105), and the
 // neighbour list of the step.
+//
+// Two phases keep the warps converged: the candidate scan only tests r < h and
+// records the pairs with 0 < r < h (the r = 0 terms -- the particle itself and
+// coincident particles -- go straight into W / rho / compression), then the
+// recorded list is walked for the kernel arithmetic.  A particle whose pairs do
+// not fit the list redoes the scan with the arithmetic inline.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_density_fluid(KConst k, FluidBuf F, BoundBuf B, int64_t n) {
+__device__ __forceinline__ void density_pair_fluid(const KConst &k, const FluidBuf &F, float4 pi, int j,
+                                                   float &wsum, float &rho, float &comp, float &a1x, float &a1y,
+                                                   float &a1z, float &a2) {
+    const float4 pj = F.pos[j];
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < k.h2) {
+        const float2 mv = F.mv[j];
+        const float r = sqrtf(r2);
+        const float q = r * k.inv_h;
+        const float w = kw(q) * k.sig;
+        wsum += w;
+        rho += w * mv.x;
+        comp += w * mv.y;
+        if (r2 > 0.f) {
+            const float wg = kwg(q) * k.sig_h;
+            const float f = pj.w * wg / r;
+            a1x += f * dx;
+            a1y += f * dy;
+            a1z += f * dz;
+            a2 += wg * wg * pj.w * pj.w / mv.x;
+        }
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void density_pair_bound(const KConst &k, const BoundBuf &B, float4 pi, int j,
+                                                   float &wsum, float &rho, float &comp, float &a1x, float &a1y,
+                                                   float &a1z) {
+    const float4 pj = B.pos[j];
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < k.h2) {
+        const float2 mv = B.mv[j];
+        const float r = sqrtf(r2);
+        const float q = r * k.inv_h;
+        const float w = kw(q) * k.sig;
+        wsum += w;
+        rho += w * mv.x;
+        comp += w * mv.y;
+        if (r2 > 0.f) {
+            const float f = pj.w * kwg(q) * k.sig_h / r;
+            a1x += f * dx;
+            a1y += f * dy;
+            a1z += f * dz;
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf F, BoundBuf B, int64_t n) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (s >= n) return;
     const float4 pi = F.pos[s];
@@ -32,28 +88,22 @@ __global__ void __launch_bounds__(kBlock) k_density_fluid(KConst k, FluidBuf F, 
     int *L = F.nbr;
     const int64_t stride = F.cap;
     const int cap = k.nbr_max;
+    const float w0 = kw(0.f) * k.sig;
     if (ok) {
+        // phase 1: record the pairs
         visit_candidates<DIM>(F.start, k, code, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (r2 < k.h2) {
-                const float2 mv = F.mv[j];
-                const float r = sqrtf(r2);
-                const float q = r * k.inv_h;
-                const float w = kw(q) * k.sig;
-                wsum += w;
-                rho += w * mv.x;
-                comp += w * mv.y;
                 if (r2 > 0.f) {
-                    const float wg = kwg(q) * k.sig_h;
-                    const float f = pj.w * wg / r;
-                    a1x += f * dx;
-                    a1y += f * dy;
-                    a1z += f * dz;
-                    a2 += wg * wg * pj.w * pj.w / mv.x;
                     if (nfl < cap) L[nbr_index(nfl, s, stride)] = j;
                     ++nfl;
+                } else {
+                    const float2 mv = F.mv[j];
+                    wsum += w0;
+                    rho += w0 * mv.x;
+                    comp += w0 * mv.y;
                 }
             }
         });
@@ -62,24 +112,33 @@ __global__ void __launch_bounds__(kBlock) k_density_fluid(KConst k, FluidBuf F, 
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (r2 < k.h2) {
-                const float2 mv = B.mv[j];
-                const float r = sqrtf(r2);
-                const float q = r * k.inv_h;
-                const float w = kw(q) * k.sig;
-                wsum += w;
-                rho += w * mv.x;
-                comp += w * mv.y;
                 if (r2 > 0.f) {
-                    const float f = pj.w * kwg(q) * k.sig_h / r;
-                    a1x += f * dx;
-                    a1y += f * dy;
-                    a1z += f * dz;
                     const int t = nfl + nbo;
                     if (t < cap) L[nbr_index(t, s, stride)] = j;
                     ++nbo;
+                } else {
+                    const float2 mv = B.mv[j];
+                    wsum += w0;
+                    rho += w0 * mv.x;
+                    comp += w0 * mv.y;
                 }
             }
         });
+        if (nfl + nbo <= cap) {
+            // phase 2: the arithmetic over the recorded pairs
+            walk_blocks<1>(F.nbr, s, stride, 0, nfl, nfl + nbo,
+                [&](int j) { density_pair_fluid<DIM>(k, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2); },
+                [&](int j) { density_pair_bound<DIM>(k, B, pi, j, wsum, rho, comp, a1x, a1y, a1z); });
+        } else {
+            // list overflow: one scan with the arithmetic inline
+            wsum = rho = comp = a2 = a1x = a1y = a1z = 0.f;
+            visit_candidates<DIM>(F.start, k, code, [&](int j) {
+                density_pair_fluid<DIM>(k, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
+            });
+            visit_candidates<DIM>(B.start, k, code, [&](int j) {
+                density_pair_bound<DIM>(k, B, pi, j, wsum, rho, comp, a1x, a1y, a1z);
+            });
+        }
     }
     F.nbr_cnt[s] = (nfl + nbo <= cap) ? ((unsigned int)nfl | ((unsigned int)nbo << 16)) : kNbrOverflow;
     const float4 mp = F.mpsi[s];
