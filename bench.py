@@ -187,6 +187,130 @@ def cpu_baseline(n_side, budget_s, max_steps):
             "ms_per_step": el / steps * 1e3, "iters": iters}
 
 
+def run_batched(n_scenes, steps, warmup, dev):
+    """Scenes of workloads.batched_dambreaks stepped (a) as one batch and (b) one at
+    a time, each through its own plain context: particle-steps/s of both."""
+    import torch
+    from tichi_sph_gb300 import sph_config, workloads, Solver
+    from tichi_sph_gb300.batch import BatchSolver, gather_scenes
+    from tichi_sph_gb300.simulation import Simulation
+    sims = []
+    for c, sc in workloads.batched_dambreaks(n_scenes):
+        cfg = sph_config.Config(c, sc)
+        sim = Simulation(cfg, device="cpu")
+        sim.init_scenario()
+        sims.append(sim)
+    fluid, bound, nf, nb = gather_scenes(sims, device=dev)
+    batch = BatchSolver([s.config for s in sims], fluid, bound, nf, nb)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        batch.substep()
+    torch.cuda.synchronize(dev)
+    s0 = batch.stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        batch.substep()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    s1 = batch.stats()
+    batch.close()
+    kd = sum(b["total_div_iter"] - a["total_div_iter"] for a, b in zip(s0, s1)) / (steps * n_scenes)
+    ki = sum(b["total_incom_iter"] - a["total_incom_iter"] for a, b in zip(s0, s1)) / (steps * n_scenes)
+    solos = [Solver(s.config, s.fluid, s.bound) for s in sims]
+    for _ in range(warmup):
+        for so in solos:
+            so.substep()
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(steps):
+        for so in solos:
+            so.substep()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms_seq = e0.elapsed_time(e1) / steps
+    for so in solos:
+        so.close()
+    tot = sum(nf)
+    return {"n_scenes": n_scenes, "fluid_particles": tot, "boundary_particles": sum(nb),
+            "value": tot / (ms / 1e3), "sequential_value": tot / (ms_seq / 1e3), "speedup": ms_seq / ms,
+            "ms_per_step": ms, "sequential_ms_per_step": ms_seq, "mean_div_iter": kd, "mean_incom_iter": ki,
+            "steps": steps, "warmup": warmup}
+
+
+def batched_line(res, args, ws):
+    return {"metric": "particle-steps/s, batched vs plain", "value": res["value"] * ws, "unit": UNIT,
+            "n_gpus": ws, "steps": res["steps"], "warmup": res["warmup"], "ms_per_step": res["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "%d independent 3D dam breaks (seed 4), fluid log-uniform in [2k, 200k], aspect "
+                                   "[0.5, 2], rest density [800, 1200], spacing 0.01" % res["n_scenes"],
+                       "fluid_particles": res["fluid_particles"], "boundary_particles": res["boundary_particles"],
+                       "sequential_value": res["sequential_value"], "speedup_vs_sequential": res["speedup"],
+                       "sequential_ms_per_step": res["sequential_ms_per_step"],
+                       "mean_div_iter": res["mean_div_iter"], "mean_incom_iter": res["mean_incom_iter"]}}
+
+
+def run_other(kind, steps, warmup, dev):
+    """The two-phase VFSPH block pair or the 2D dam break through the plain path."""
+    import numpy as np
+    import torch
+    from tichi_sph_gb300 import sph_config, workloads
+    from tichi_sph_gb300.simulation import Simulation
+    if kind == "twophase3d":
+        c, sc, noise = workloads.twophase_3d()
+        fbm = True
+    else:
+        c, sc = workloads.dambreak_2d()
+        noise, fbm = None, False
+    cfg = sph_config.Config(c, sc)
+    sim = Simulation(cfg, device=dev, fbm=fbm)
+    sim.init_scenario()
+    nf = sim.fluid.part_num[None]
+    if noise is not None:
+        vf = noise(sim.fluid.volume_frac[:nf].cpu().numpy())
+        sim.fluid.volume_frac[:nf] = torch.as_tensor(vf, device=dev)
+        sim.fluid.update_mass_all()
+    s = sim.solver
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        s.substep()
+    torch.cuda.synchronize(dev)
+    s0 = s.stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        s.substep()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    s1 = s.stats()
+    vf = sim.fluid.volume_frac[:nf].cpu().numpy().astype(np.float64)
+    s.close()
+    return {"kind": kind, "fluid_particles": nf, "boundary_particles": sim.bound.part_num[None], "ms": ms,
+            "steps": steps, "warmup": warmup,
+            "div": (s1["total_div_iter"] - s0["total_div_iter"]) / steps,
+            "inc": (s1["total_incom_iter"] - s0["total_incom_iter"]) / steps,
+            "fbm": (s1["total_fbm_passes"] - s0["total_fbm_passes"]) / steps,
+            "max_comp": s1["max_dens_compression"], "vf_sum_err": float(np.abs(vf.sum(axis=1) - 1).max()),
+            "vf_min": float(vf.min())}
+
+
+def other_line(res, args, ws):
+    desc = {"twophase3d": "3D two-phase VFSPH, two 1 m cubes (rest density 1000 / 500) of 1M particles each, "
+                          "spacing 0.01, surface tension 0.07, volume-fraction update on",
+            "dambreak2d": "2D DFSPH dam break, 1.0 x 2.0 m block at 0.02 m (5,000 particles), 4 x 4 m box, "
+                          "dt 1e-3"}[res["kind"]]
+    return {"metric": METRIC, "value": res["fluid_particles"] * ws / (res["ms"] / 1e3), "unit": UNIT, "n_gpus": ws,
+            "steps": res["steps"], "warmup": res["warmup"], "ms_per_step": res["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "fluid_particles": res["fluid_particles"],
+                       "boundary_particles": res["boundary_particles"], "mean_div_iter": res["div"],
+                       "mean_incom_iter": res["inc"], "mean_fbm_passes": res["fbm"],
+                       "max_density_error": res["max_comp"], "max_abs_volume_fraction_sum_error": res["vf_sum_err"],
+                       "min_volume_fraction": res["vf_min"]}}
+
+
 def run_reference(args, rank, ws):
     if rank != 0:
         return 0
@@ -224,6 +348,11 @@ def main():
                          "as profilers list them)")
     ap.add_argument("--no-profile", action="store_true", help="skip the per-phase timing (roofline)")
     ap.add_argument("--tpp", type=int, default=0, help="threads per particle (0: autotune after warm-up)")
+    ap.add_argument("--workload", default="dambreak3d", choices=["dambreak3d", "batched", "twophase3d", "dambreak2d"],
+                    help="dambreak3d: the headline line; the others print their own line")
+    ap.add_argument("--batch-scenes", type=int, default=256,
+                    help="scenes of the batched measurement added to the headline line (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=10)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist, rank, ws = _dist()
@@ -237,6 +366,20 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.workload == "batched":
+        res = run_batched(256, args.steps, args.warmup, dev)
+        if rank == 0:
+            print(json.dumps(batched_line(res, args, ws)), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    if args.workload in ("twophase3d", "dambreak2d"):
+        res = run_other(args.workload, args.steps, args.warmup, dev)
+        if rank == 0:
+            print(json.dumps(other_line(res, args, ws)), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return 0
     cfg, sim = build_sim(args.n_side, dev)
     solver = sim.solver
     if args.hostloop:
@@ -347,6 +490,17 @@ def main():
         e2e = {"value": nf * args.steps * ws / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": ems / args.steps, "host_wall_s": wall}
 
+    batched = None
+    if args.batch_scenes > 0:
+        solver.close()
+        b = run_batched(args.batch_scenes, args.batch_steps, 3, dev)
+        batched = {k: b[k] for k in ("n_scenes", "fluid_particles", "boundary_particles", "value", "sequential_value",
+                                     "speedup", "ms_per_step", "sequential_ms_per_step", "mean_div_iter",
+                                     "mean_incom_iter")}
+        batched["unit"] = UNIT
+        batched["workload"] = ("%d independent 3D dam breaks, fluid counts log-uniform in [2k, 200k] (seed 4), "
+                               "batched in one launch vs stepped one at a time through the plain path" % b["n_scenes"])
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(args.n_side, budget_s=args.cpu_budget, max_steps=20)
@@ -371,6 +525,7 @@ def main():
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     solver.close()

@@ -135,6 +135,16 @@ typedef struct tsph_ctx tsph_ctx;
  * (sph_obj.py:281-293) plus the solver fields of Fluid.  Returns TSPH_OK. */
 int tsph_create(const tsph_params *params, int64_t fluid_capacity, int64_t bound_capacity,
                 tsph_ctx **out);
+
+/* A context that steps n_scenes independent scenes in the same launches (the
+ * batched form; the reference runs one scene per process, main.py:8-12).  Scene
+ * s has its own parameters (box, grid, rest densities, thresholds ...; dim,
+ * phase_num, solver_type, neighb_range and fbm_enabled must be equal) and its own
+ * dt, solver loops and iteration counts, as if it ran alone.  Its particles are
+ * fluid_counts[s] / bound_counts[s] consecutive entries of the caller's fluid and
+ * boundary sets, in scene order; the sets' n must equal the count totals. */
+int tsph_create_batch(const tsph_params *scenes, int n_scenes, const int64_t *fluid_counts,
+                      const int64_t *bound_counts, tsph_ctx **out);
 int tsph_destroy(tsph_ctx *ctx);
 
 /* Selects how the two solver loops run: 1 = one CUDA graph per substep with
@@ -159,11 +169,14 @@ int tsph_sph_step(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, v
 /* One substep of run_step (main.py:348-352): cfl_condition, clock, sph_step. */
 int tsph_substep(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, void *stream);
 
-/* Synchronises `stream` and copies the scalars of the last step. */
+/* Synchronises `stream` and copies the scalars of the last step (scene 0). */
 int tsph_read_stats(tsph_ctx *ctx, tsph_stats *out, void *stream);
 
-/* Sets the persistent device scalars (clock, dt, the carried-over compression
- * that the first divergence-loop test reads, main.py:201). */
+/* The same for scenes [first, first + count) of a batch, into out[count]. */
+int tsph_read_scene_stats(tsph_ctx *ctx, int first, int count, tsph_stats *out, void *stream);
+
+/* Sets the persistent device scalars of every scene (clock, dt, the carried-over
+ * compression that the first divergence-loop test reads, main.py:201). */
 int tsph_set_state(tsph_ctx *ctx, double time_count, float dt, double compression, void *stream);
 
 /* Debug / parity: builds the grid for the current positions and writes, per

@@ -71,6 +71,7 @@ CtxP = C.POINTER(Ctx)
 # name -> (restype, argtypes); the full list of symbols include/tichi_sph.h declares
 SIGNATURES = {
     "tsph_create": (C.c_int, [C.POINTER(Params), _i64, _i64, C.POINTER(CtxP)]),
+    "tsph_create_batch": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(CtxP)]),
     "tsph_destroy": (C.c_int, [CtxP]),
     "tsph_set_graph_mode": (C.c_int, [CtxP, C.c_int]),
     "tsph_set_threads_per_particle": (C.c_int, [CtxP, C.c_int]),
@@ -78,6 +79,7 @@ SIGNATURES = {
     "tsph_sph_step": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p]),
     "tsph_substep": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p]),
     "tsph_read_stats": (C.c_int, [CtxP, C.POINTER(Stats), C.c_void_p]),
+    "tsph_read_scene_stats": (C.c_int, [CtxP, C.c_int, C.c_int, C.POINTER(Stats), C.c_void_p]),
     "tsph_set_state": (C.c_int, [CtxP, C.c_double, C.c_float, C.c_double, C.c_void_p]),
     "tsph_neighbor_stats": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), _ip, C.POINTER(C.c_uint64),
                                       _ip, C.POINTER(C.c_uint64), C.c_void_p]),

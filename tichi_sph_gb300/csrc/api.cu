@@ -8,6 +8,10 @@
 // the loop body, so a substep runs without any host round trip.  The host-driven
 // mode (tsph_set_graph_mode(ctx, 0)) replays the same kernels with a
 // device-to-host read of the loop condition per iteration, as the reference does.
+//
+// A batch context steps many independent scenes in the same launches: every
+// scene keeps its own constants, time step, solver loop state and iteration
+// counts, exactly as if it ran alone, and the loops run while any scene does.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -59,47 +63,41 @@ struct Alloc {
 
 struct CtxExtra {
     Alloc alloc;
+    std::vector<void *> pinned;
     cudaStream_t cap_stream = nullptr;
     cudaStream_t body_stream = nullptr;
 };
 
-CtxExtra *extra(tsph_ctx *c);
+// The extra host state lives right after the public struct in one allocation.
+struct CtxBox {
+    tsph_ctx c;
+    CtxExtra x;
+};
 
-__global__ void k_set_state(DevPersist *dp, double time_count, float dt, double compression) {
-    dp->time_count = time_count;
-    dp->dt = dt;
-    dp->compression = compression;
+CtxExtra *extra(tsph_ctx *c) { return &reinterpret_cast<CtxBox *>(c)->x; }
+
+__global__ void k_set_state(KConst k, double time_count, float dt, double compression) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < k.n_scenes; s += gridDim.x * blockDim.x) {
+        k.sp[s].time_count = time_count;
+        k.sp[s].dt = dt;
+        k.sp[s].compression = compression;
+    }
 }
 
-// Solve with no fluid particle: the reference still runs min(iter_min, iter_max+1)
-// empty iterations and compression becomes 0/0 = NaN (sph.py:226).
-__global__ void k_solve_empty(KConst k, DevStep *ds, DevPersist *dp, int kind) {
-    int it = 0;
-    bool any = false;
-    while (it < k.iter_min) {
-        any = true;
-        ++it;
-        if (it > k.iter_max) break;
-    }
-    if (any) dp->compression = __longlong_as_double(0x7ff8000000000000ll);
-    if (kind == kSolveDiv) ds->div_iter = it;
-    else ds->incom_iter = it;
-}
-
-int solve(tsph_ctx &c, int64_t nf, int kind, cudaStream_t st, bool graph) {
-    if (nf <= 0) {
-        k_solve_empty<<<1, 1, 0, st>>>(c.k, c.ds, c.dp, kind);
-        c.launches += 1;
-        return TSPH_OK;
-    }
+// A device-side while loop: `begin` sets the condition, `body` is one iteration
+// whose last block updates it.  Graph mode captures a conditional while node;
+// host mode reads the condition back before every iteration.
+template <class Begin, class Body>
+int while_loop(tsph_ctx &c, cudaStream_t st, bool graph, const int32_t *dev_flag, int32_t *host_flag, Begin begin,
+               Body body) {
     if (!graph) {
-        launch_solve_begin(c, kind, 0, 0, st);
+        begin(0, 0, st);
         for (;;) {
-            TSPH_CK(cudaMemcpyAsync(&c.host_ds->cond, &c.ds->cond, sizeof(int), cudaMemcpyDeviceToHost, st));
+            TSPH_CK(cudaMemcpyAsync(host_flag, dev_flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
             TSPH_CK(cudaStreamSynchronize(st));
-            if (!c.host_ds->cond) break;
+            if (!*host_flag) break;
             const int save = c.launches;  // loop-body launches are counted per iteration
-            launch_solve_iter(c, nf, kind, 0, 0, st);
+            body(0, 0, st);
             c.launches = save;
         }
         return TSPH_OK;
@@ -112,7 +110,7 @@ int solve(tsph_ctx &c, int64_t nf, int kind, cudaStream_t st, bool graph) {
     TSPH_CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &ed, &nd));
     cudaGraphConditionalHandle h;
     TSPH_CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
-    launch_solve_begin(c, kind, h, 1, st);
+    begin(h, 1, st);
     TSPH_CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &ed, &nd));
     cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
     np.conditional.handle = h;
@@ -121,56 +119,29 @@ int solve(tsph_ctx &c, int64_t nf, int kind, cudaStream_t st, bool graph) {
     cudaGraphNode_t node;
     TSPH_CK(cudaGraphAddNode(&node, g, deps, ed, nd, &np));
     TSPH_CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-    cudaGraph_t body = np.conditional.phGraph_out[0];
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
     cudaStream_t bs = extra(&c)->body_stream;
-    TSPH_CK(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    TSPH_CK(cudaStreamBeginCaptureToGraph(bs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     const int save = c.launches;
-    launch_solve_iter(c, nf, kind, h, 1, bs);
+    body(h, 1, bs);
     c.launches = save;
     cudaGraph_t tmp;
     TSPH_CK(cudaStreamEndCapture(bs, &tmp));
     return TSPH_OK;
 }
 
-int fbm_loop(tsph_ctx &c, int64_t nf, cudaStream_t st, bool graph) {
-    if (!graph) {
-        launch_fbm_begin(c, nf, 0, 0, st);
-        for (;;) {
-            TSPH_CK(cudaMemcpyAsync(&c.host_ds->fbm_cond, &c.ds->fbm_cond, sizeof(int), cudaMemcpyDeviceToHost, st));
-            TSPH_CK(cudaStreamSynchronize(st));
-            if (!c.host_ds->fbm_cond) break;
-            const int save = c.launches;
-            launch_fbm_pass(c, nf, 0, 0, st);
-            c.launches = save;
-        }
-        return TSPH_OK;
-    }
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t g;
-    const cudaGraphNode_t *deps = nullptr;
-    const cudaGraphEdgeData *ed = nullptr;
-    size_t nd = 0;
-    TSPH_CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &ed, &nd));
-    cudaGraphConditionalHandle h;
-    TSPH_CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
-    launch_fbm_begin(c, nf, h, 1, st);
-    TSPH_CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &ed, &nd));
-    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    TSPH_CK(cudaGraphAddNode(&node, g, deps, ed, nd, &np));
-    TSPH_CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-    cudaGraph_t body = np.conditional.phGraph_out[0];
-    cudaStream_t bs = extra(&c)->body_stream;
-    TSPH_CK(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    const int save = c.launches;
-    launch_fbm_pass(c, nf, h, 1, bs);
-    c.launches = save;
-    cudaGraph_t tmp;
-    TSPH_CK(cudaStreamEndCapture(bs, &tmp));
-    return TSPH_OK;
+int solve(tsph_ctx &c, int kind, cudaStream_t st, bool graph) {
+    return while_loop(
+        c, st, graph, &c.k.dg->cond_any, &c.host_dg->cond_any,
+        [&](cudaGraphConditionalHandle h, int u, cudaStream_t s) { launch_solve_begin(c, kind, h, u, s); },
+        [&](cudaGraphConditionalHandle h, int u, cudaStream_t s) { launch_solve_iter(c, kind, h, u, s); });
+}
+
+int fbm_loop(tsph_ctx &c, cudaStream_t st, bool graph) {
+    return while_loop(
+        c, st, graph, &c.k.dg->fbm_any, &c.host_dg->fbm_any,
+        [&](cudaGraphConditionalHandle h, int u, cudaStream_t s) { launch_fbm_begin(c, h, u, s); },
+        [&](cudaGraphConditionalHandle h, int u, cudaStream_t s) { launch_fbm_pass(c, h, u, s); });
 }
 
 // Enqueues one step (optionally preceded by cfl_condition) on `st`.
@@ -179,14 +150,14 @@ int enqueue_step(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t
     launch_step_begin(c, st);
     if (with_cfl) launch_cfl(c, f, st);
     launch_grid_build(c, f, b, st);
-    launch_density(c, f.n, b.n, st);
-    int rc = solve(c, f.n, kSolveDiv, st, graph);
+    launch_density(c, st);
+    int rc = solve(c, kSolveDiv, st, graph);
     if (rc) return rc;
-    launch_advect(c, f.n, st);
-    rc = solve(c, f.n, kSolveDens, st, graph);
+    launch_advect(c, st);
+    rc = solve(c, kSolveDens, st, graph);
     if (rc) return rc;
     if (c.p.fbm_enabled) {
-        rc = fbm_loop(c, f.n, st, graph);
+        rc = fbm_loop(c, st, graph);
         if (rc) return rc;
     }
     launch_unsort(c, f, b, st);
@@ -211,13 +182,38 @@ void set_key(const tsph_set &f, const tsph_set &b, int with_cfl, unsigned long l
     out[3] = ((unsigned long long)b.n << 1) | (unsigned long long)with_cfl;
 }
 
-int run_step(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream, bool with_cfl) {
+// Validates the caller's sets against the context and, for a single-scene
+// context, makes the scene's particle counts follow them (inlets add particles).
+int bind_sets(tsph_ctx *c, const tsph_set *f, const tsph_set *b) {
     if (!c || !f || !b) return fail(TSPH_ERR_INVALID, "null argument");
-    if (f->n < 0 || b->n < 0 || f->n > c->F.cap || b->n > c->B.cap)
+    if (f->n < 0 || b->n < 0) return fail(TSPH_ERR_INVALID, "negative part_num");
+    SceneConst &h = c->host_sc[0];
+    if (c->batch) {
+        long long tf = 0, tb = 0;
+        for (int s = 0; s < c->n_scenes; ++s) {
+            tf += c->host_sc[s].f_n;
+            tb += c->host_sc[s].b_n;
+        }
+        if (f->n != tf || b->n != tb)
+            return fail(TSPH_ERR_CAPACITY, "particle counts differ from the scene counts given at tsph_create_batch");
+        return TSPH_OK;
+    }
+    if (f->n > h.f_slots || b->n > h.b_slots)
         return fail(TSPH_ERR_CAPACITY, "part_num above the capacity given at tsph_create");
+    if (f->n != h.f_n || b->n != h.b_n) {
+        h.f_n = f->n;
+        h.b_n = b->n;
+        TSPH_CK(cudaMemcpy((void *)c->k.sc, c->host_sc, sizeof(SceneConst), cudaMemcpyHostToDevice));
+    }
+    return TSPH_OK;
+}
+
+int run_step(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream, bool with_cfl) {
+    int rc = bind_sets(c, f, b);
+    if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     if (!c->use_graph) {
-        int rc = enqueue_step(*c, *f, *b, st, with_cfl, false);
+        rc = enqueue_step(*c, *f, *b, st, with_cfl, false);
         if (rc) return rc;
         TSPH_CK(cudaGetLastError());
         c->stepped++;
@@ -232,7 +228,7 @@ int run_step(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream, bo
         }
         cudaStream_t cap = extra(c)->cap_stream;
         TSPH_CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_step(*c, *f, *b, cap, with_cfl, true);
+        rc = enqueue_step(*c, *f, *b, cap, with_cfl, true);
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamEndCapture(cap, &graph);
         if (rc) {
@@ -253,25 +249,266 @@ int run_step(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream, bo
     return TSPH_OK;
 }
 
+// SceneConst of one scene from its parameters.
+void make_scene(const tsph_params &p, SceneConst &c) {
+    std::memset(&c, 0, sizeof(c));
+    for (int d = 0; d < 3; ++d) {
+        c.lb[d] = d < p.dim ? p.lb[d] : 0.f;
+        c.g[d] = d < p.dim ? p.gravity[d] : 0.f;
+    }
+    c.h = p.kernel_h;
+    c.h2 = p.kernel_h2;
+    c.inv_h = 1.f / p.kernel_h;
+    c.sig = p.kernel_sig;
+    c.sig_h = p.kernel_sig / p.kernel_h;
+    c.c_coh = (float)(32.0 / 3.14159265358979323846 / ((double)p.kernel_h * p.kernel_h * p.kernel_h));
+    c.node_num = p.node_num;
+    c.nx = p.grid_size[0];
+    c.nxny = (long long)p.grid_size[0] * (p.dim == 3 ? p.grid_size[1] : 1);
+    c.mu = p.viscosity;
+    c.gamma = p.surface_tension_gamma;
+    c.fbm_c = p.fbm_convection;
+    c.fbm_D = p.fbm_diffusion;
+    for (int q = 0; q < kMaxP; ++q) c.rho_phase[q] = q < p.phase_num ? p.phase_rest_density[q] : 0.f;
+    c.part_size = p.part_size;
+    c.cfl = p.cfl_factor;
+    c.cs = p.cs;
+    c.iter_min = p.iter_min;
+    c.iter_max = p.iter_max;
+    c.fbm_max_passes = p.fbm_max_passes > 0 ? p.fbm_max_passes : 1000;
+    c.div_tol = p.divergence_threshold;
+    c.comp_tol = p.compression_threshold;
+}
+
+int check_params(const tsph_params &p) {
+    if (p.dim != 2 && p.dim != 3) return fail(TSPH_ERR_INVALID, "dim must be 2 or 3");
+    if (p.phase_num < 1 || p.phase_num > TSPH_MAX_PHASES) return fail(TSPH_ERR_INVALID, "phase_num out of range");
+    if (p.neighb_range < 0 || p.neighb_range > 8) return fail(TSPH_ERR_INVALID, "neighb_range out of range");
+    if (!(p.kernel_h > 0.f)) return fail(TSPH_ERR_INVALID, "kernel_h must be positive");
+    if (p.node_num < 1 || p.node_num > 0x7ffffff0ll) return fail(TSPH_ERR_INVALID, "node_num out of range");
+    if (p.cs == 0) return fail(TSPH_ERR_INVALID, "solver_cs must be nonzero");
+    return TSPH_OK;
+}
+
+long long round_chunk(long long n) { return (n + kChunk - 1) / kChunk * kChunk; }
+
+// Builds a context for S scenes.  batch = 0: one scene whose particle counts
+// follow the caller's sets up to the capacities; batch = 1: fixed counts.
+int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *bn, int batch, int64_t capf,
+                int64_t capb, tsph_ctx **out) {
+    if (!ps || !out || S < 1) return fail(TSPH_ERR_INVALID, "null argument or no scene");
+    *out = nullptr;
+    for (int s = 0; s < S; ++s) {
+        int rc = check_params(ps[s]);
+        if (rc) return rc;
+        if (ps[s].dim != ps[0].dim || ps[s].phase_num != ps[0].phase_num ||
+            ps[s].solver_type != ps[0].solver_type || ps[s].neighb_range != ps[0].neighb_range ||
+            ps[s].fbm_enabled != ps[0].fbm_enabled)
+            return fail(TSPH_ERR_INVALID, "scenes of a batch must share dim, phase_num, solver_type, "
+                                          "neighb_range and fbm_enabled");
+        if (batch && (fn[s] < 0 || bn[s] < 0)) return fail(TSPH_ERR_INVALID, "negative scene particle count");
+    }
+    if (!batch && (capf < 0 || capb < 0)) return fail(TSPH_ERR_INVALID, "negative capacity");
+    CtxBox *box = new (std::nothrow) CtxBox();
+    if (!box) return fail(TSPH_ERR_INVALID, "out of host memory");
+    tsph_ctx &c = box->c;
+    Alloc &A = box->x.alloc;
+    c.p = ps[0];
+    c.n_scenes = S;
+    c.batch = batch;
+    c.tpp = 1;
+    c.use_graph = 1;
+
+    std::vector<SceneConst> sc(S);
+    long long cbase = 0, fslot = 0, bslot = 0, fuser = 0, buser = 0;
+    int st_on = 0;
+    for (int s = 0; s < S; ++s) {
+        make_scene(ps[s], sc[s]);
+        sc[s].cbase = cbase;
+        cbase += ps[s].node_num;
+        const long long nf = batch ? fn[s] : 0, nb = batch ? bn[s] : 0;
+        sc[s].f_user = fuser;
+        sc[s].b_user = buser;
+        sc[s].f_n = nf;
+        sc[s].b_n = nb;
+        sc[s].f_slot = fslot;
+        sc[s].b_slot = bslot;
+        sc[s].f_slots = round_chunk(batch ? nf : (capf > 0 ? capf : 1));
+        sc[s].b_slots = round_chunk(batch ? nb : (capb > 0 ? capb : 1));
+        fslot += sc[s].f_slots;
+        bslot += sc[s].b_slots;
+        fuser += batch ? nf : capf;
+        buser += batch ? nb : capb;
+        if (ps[s].surface_tension_gamma != 0.f) st_on = 1;
+    }
+    if (cbase > 0x7ffffff0ll) {
+        delete box;
+        return fail(TSPH_ERR_INVALID, "total grid cells of the batch exceed 2^31");
+    }
+    c.st_on = st_on;
+    // at least one chunk per set, owned by a scene without particles of that set
+    const long long fcap = fslot > 0 ? fslot : kChunk, bcap = bslot > 0 ? bslot : kChunk;
+    const long long nn = cbase, P = ps[0].phase_num;
+    KConst &k = c.k;
+    k.dim = ps[0].dim;
+    k.P = ps[0].phase_num;
+    k.vfsph = ps[0].solver_type == TSPH_VFSPH ? 1 : 0;
+    k.R = ps[0].neighb_range;
+    k.nbr_max = ps[0].dim == 3 ? 64 : 32;  // a multiple of 4 (blocked layout)
+    k.n_scenes = S;
+    k.total_nodes = nn;
+    k.f_slots = fcap;
+    k.b_slots = bcap;
+
+    std::vector<int> fchunk(fcap / kChunk, 0), bchunk(bcap / kChunk, 0);
+    std::vector<int> fus(fuser > 0 ? fuser : 1, 0), bus(buser > 0 ? buser : 1, 0);
+    std::vector<long long> cb(S + 1);
+    for (int s = 0; s < S; ++s) {
+        for (long long i = sc[s].f_slot / kChunk; i < (sc[s].f_slot + sc[s].f_slots) / kChunk; ++i) fchunk[i] = s;
+        for (long long i = sc[s].b_slot / kChunk; i < (sc[s].b_slot + sc[s].b_slots) / kChunk; ++i) bchunk[i] = s;
+        const long long fu = batch ? sc[s].f_n : capf, bu = batch ? sc[s].b_n : capb;
+        for (long long i = 0; i < fu; ++i) fus[sc[s].f_user + i] = s;
+        for (long long i = 0; i < bu; ++i) bus[sc[s].b_user + i] = s;
+        cb[s] = sc[s].cbase;
+    }
+    if (fslot == 0)  // all scenes are without fluid: the chunk belongs to one of them
+        for (auto &v : fchunk) v = 0;
+    cb[S] = nn;
+
+    FluidBuf &F = c.F;
+    F.cap = fcap;
+    F.count = A.get<int>(nn);
+    F.start = A.get<int>(nn + 1);
+    F.slot = A.get<int>((long long)fus.size());
+    F.inv = A.get<int>((long long)fus.size());
+    F.perm = A.get<int>(fcap);
+    F.pos = A.get<float4>(fcap);
+    F.mv = A.get<float2>(fcap);
+    F.mpsi = A.get<float4>(fcap);
+    F.rho0 = A.get<float>(fcap);
+    F.vel = A.get<float4>(fcap);
+    F.vadv = A.get<float4>(2 * fcap);
+    F.psiadv = A.get<float>(fcap);
+    F.kappa = A.get<float>(fcap);
+    F.acc = A.get<float4>(fcap);
+    F.normal = A.get<float4>(fcap);
+    F.W = A.get<float>(fcap);
+    F.rho = A.get<float>(fcap);
+    F.comp = A.get<float>(fcap);
+    F.a2 = A.get<float>(fcap);
+    F.a1 = A.get<float4>(fcap);
+    F.vf = A.get<float>(P * fcap);
+    F.vftmp = A.get<float>(P * fcap);
+    F.drift = A.get<float4>(P * fcap);
+    F.facc = A.get<float4>(fcap);
+    F.zeta = A.get<float>(fcap);
+    F.flagpass = A.get<int>(fcap);
+    F.nbr = A.get<int>((long long)k.nbr_max * fcap);
+    F.nbr_cnt = A.get<unsigned int>(fcap);
+    BoundBuf &B = c.B;
+    B.cap = bcap;
+    B.count = A.get<int>(nn);
+    B.start = A.get<int>(nn + 1);
+    B.slot = A.get<int>((long long)bus.size());
+    B.inv = A.get<int>((long long)bus.size());
+    B.perm = A.get<int>(bcap);
+    B.pos = A.get<float4>(bcap);
+    B.mv = A.get<float2>(bcap);
+    B.vadv = A.get<float4>(bcap);
+    B.kappa = A.get<float>(bcap);
+    B.W = A.get<float>(bcap);
+    B.rho = A.get<float>(bcap);
+    B.comp = A.get<float>(bcap);
+    B.a2 = A.get<float>(bcap);
+    B.alpha = A.get<float>(bcap);
+    c.S.partials_len = 2 * 8 * ((fcap + bcap) / kBlock) + 64;  // up to 8 threads per particle
+    c.S.partials = A.get<double>(c.S.partials_len);
+    const int64_t nscan = (nn + 4095) / 4096 + 1;
+    c.S.scan_len = 2 * nscan;
+    c.S.scan_blocks = A.get<int>(c.S.scan_len);
+    SceneConst *d_sc = A.get<SceneConst>(S);
+    k.sp = A.get<ScenePersist>(S);
+    k.ss = A.get<SceneStep>(S);
+    k.dg = A.get<DevGlobal>(1);
+    int *d_fchunk = A.get<int>((long long)fchunk.size());
+    int *d_bchunk = A.get<int>((long long)bchunk.size());
+    int *d_fus = A.get<int>((long long)fus.size());
+    int *d_bus = A.get<int>((long long)bus.size());
+    long long *d_cb = A.get<long long>(S + 1);
+    k.sc = d_sc;
+    k.f_chunk_scene = d_fchunk;
+    k.b_chunk_scene = d_bchunk;
+    k.f_user_scene = d_fus;
+    k.b_user_scene = d_bus;
+    k.cbase_list = d_cb;
+    cudaError_t e = A.err;
+    if (e == cudaSuccess) e = cudaMemcpy(d_sc, sc.data(), sizeof(SceneConst) * S, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_fchunk, fchunk.data(), sizeof(int) * fchunk.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_bchunk, bchunk.data(), sizeof(int) * bchunk.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_fus, fus.data(), sizeof(int) * fus.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_bus, bus.data(), sizeof(int) * bus.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_cb, cb.data(), sizeof(long long) * (S + 1), cudaMemcpyHostToDevice);
+    void *hp = nullptr;
+    if (e == cudaSuccess) e = cudaMallocHost(&hp, sizeof(SceneConst) * S);
+    if (e == cudaSuccess) {
+        box->x.pinned.push_back(hp);
+        c.host_sc = (SceneConst *)hp;
+        std::memcpy(c.host_sc, sc.data(), sizeof(SceneConst) * S);
+        e = cudaMallocHost(&hp, sizeof(SceneStep) * S);
+    }
+    if (e == cudaSuccess) {
+        box->x.pinned.push_back(hp);
+        c.host_ss = (SceneStep *)hp;
+        e = cudaMallocHost(&hp, sizeof(ScenePersist) * S);
+    }
+    if (e == cudaSuccess) {
+        box->x.pinned.push_back(hp);
+        c.host_sp = (ScenePersist *)hp;
+        e = cudaMallocHost(&hp, sizeof(DevGlobal));
+    }
+    if (e == cudaSuccess) {
+        box->x.pinned.push_back(hp);
+        c.host_dg = (DevGlobal *)hp;
+        e = cudaStreamCreateWithFlags(&box->x.cap_stream, cudaStreamNonBlocking);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&box->x.body_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        int rc = fail_cuda(e, "tsph_create");
+        tsph_destroy(&c);
+        return rc;
+    }
+    *out = &c;
+    return TSPH_OK;
+}
+
+void fill_stats(const tsph_ctx *c, int s, tsph_stats *out) {
+    const SceneStep &st = c->host_ss[s];
+    const ScenePersist &d = c->host_sp[s];
+    std::memset(out, 0, sizeof(*out));
+    out->dt = d.dt;
+    out->time_count = d.time_count;
+    out->compression = d.compression;
+    out->kinetic_energy = st.kinetic_energy;
+    out->potential_energy = st.potential_energy;
+    out->div_iter = st.div_iter;
+    out->incom_iter = st.incom_iter;
+    out->fbm_passes = st.fbm_passes;
+    out->general_flag = c->p.fbm_enabled ? st.gflag_out : 1;
+    out->status = st.status;
+    out->fluid_in_grid = st.f_in;
+    out->bound_in_grid = st.b_in;
+    out->steps = d.steps;
+    out->total_div_iter = d.total_div_iter;
+    out->total_incom_iter = d.total_incom_iter;
+    out->total_fbm_passes = d.total_fbm_passes;
+    out->max_dens_compression = d.max_dens_compression;
+    out->launches_per_step = c->launches_per_step;
+    out->launches_per_iter = 2;
+    out->launches_per_pass = 1;
+}
+
 }  // namespace
-
-// The extra host state lives right after the public struct in one allocation.
-struct CtxBox {
-    tsph_ctx c;
-    CtxExtra x;
-};
-
-namespace {
-CtxExtra *extra(tsph_ctx *c) { return &reinterpret_cast<CtxBox *>(c)->x; }
-}  // namespace
-
-extern "C" {
-
-const char *tsph_version(void) { return "tichi_sph_gb300 0.1 (sm_103a)"; }
-
-const char *tsph_last_error(void) { return g_last_error; }
-
-}  // extern "C"
 
 namespace tsph {
 // Lets other translation units report through tsph_last_error.
@@ -280,131 +517,26 @@ void set_last_error_text(const char *msg) { std::snprintf(g_last_error, sizeof(g
 
 extern "C" {
 
-int tsph_create(const tsph_params *p, int64_t capf, int64_t capb, tsph_ctx **out) {
-    if (!p || !out) return fail(TSPH_ERR_INVALID, "null argument");
-    *out = nullptr;
-    if (p->dim != 2 && p->dim != 3) return fail(TSPH_ERR_INVALID, "dim must be 2 or 3");
-    if (p->phase_num < 1 || p->phase_num > TSPH_MAX_PHASES) return fail(TSPH_ERR_INVALID, "phase_num out of range");
-    if (p->neighb_range < 0 || p->neighb_range > 8) return fail(TSPH_ERR_INVALID, "neighb_range out of range");
-    if (!(p->kernel_h > 0.f)) return fail(TSPH_ERR_INVALID, "kernel_h must be positive");
-    if (p->node_num < 1 || p->node_num > 0x7ffffff0ll) return fail(TSPH_ERR_INVALID, "node_num out of range");
-    if (capf < 0 || capb < 0 || capf > 0x7ffffff0ll || capb > 0x7ffffff0ll)
-        return fail(TSPH_ERR_INVALID, "capacity out of range");
-    if (p->cs == 0) return fail(TSPH_ERR_INVALID, "solver_cs must be nonzero");
-    CtxBox *box = new (std::nothrow) CtxBox();
-    if (!box) return fail(TSPH_ERR_INVALID, "out of host memory");
-    tsph_ctx &c = box->c;
-    Alloc &A = box->x.alloc;
-    c.p = *p;
-    KConst &k = c.k;
-    for (int d = 0; d < 3; ++d) {
-        k.lb[d] = d < p->dim ? p->lb[d] : 0.f;
-        k.g[d] = d < p->dim ? p->gravity[d] : 0.f;
-    }
-    k.h = p->kernel_h;
-    k.h2 = p->kernel_h2;
-    k.inv_h = 1.f / p->kernel_h;
-    k.sig = p->kernel_sig;
-    k.sig_h = p->kernel_sig / p->kernel_h;
-    k.node_num = p->node_num;
-    k.nx = p->grid_size[0];
-    k.nxny = (long long)p->grid_size[0] * (p->dim == 3 ? p->grid_size[1] : 1);
-    k.R = p->neighb_range;
-    k.dim = p->dim;
-    k.P = p->phase_num;
-    k.vfsph = p->solver_type == TSPH_VFSPH ? 1 : 0;
-    k.mu = p->viscosity;
-    k.gamma = p->surface_tension_gamma;
-    k.fbm_c = p->fbm_convection;
-    k.fbm_D = p->fbm_diffusion;
-    for (int q = 0; q < kMaxP; ++q) k.rho_phase[q] = q < p->phase_num ? p->phase_rest_density[q] : 0.f;
-    k.part_size = p->part_size;
-    k.cfl = p->cfl_factor;
-    k.cs = p->cs;
-    k.iter_min = p->iter_min;
-    k.iter_max = p->iter_max;
-    k.fbm_max_passes = p->fbm_max_passes > 0 ? p->fbm_max_passes : 1000;
-    k.div_tol = p->divergence_threshold;
-    k.comp_tol = p->compression_threshold;
-    k.c_coh = (float)(32.0 / 3.14159265358979323846 / ((double)p->kernel_h * p->kernel_h * p->kernel_h));
+const char *tsph_version(void) { return "tichi_sph_gb300 0.2 (sm_103a)"; }
 
-    const int64_t nn = p->node_num, P = p->phase_num;
-    if (capf < 1) capf = 1;
-    if (capb < 1) capb = 1;
-    FluidBuf &F = c.F;
-    F.cap = capf;
-    F.count = A.get<int>(nn);
-    F.start = A.get<int>(nn + 1);
-    F.slot = A.get<int>(capf);
-    F.perm = A.get<int>(capf);
-    F.inv = A.get<int>(capf);
-    F.pos = A.get<float4>(capf);
-    F.mv = A.get<float2>(capf);
-    F.mpsi = A.get<float4>(capf);
-    F.rho0 = A.get<float>(capf);
-    F.vel = A.get<float4>(capf);
-    F.vadv = A.get<float4>(2 * capf);
-    F.psiadv = A.get<float>(capf);
-    F.kappa = A.get<float>(capf);
-    F.acc = A.get<float4>(capf);
-    F.normal = A.get<float4>(capf);
-    F.W = A.get<float>(capf);
-    F.rho = A.get<float>(capf);
-    F.comp = A.get<float>(capf);
-    F.a2 = A.get<float>(capf);
-    F.a1 = A.get<float4>(capf);
-    F.vf = A.get<float>(P * capf);
-    F.vftmp = A.get<float>(P * capf);
-    F.drift = A.get<float4>(P * capf);
-    F.facc = A.get<float4>(capf);
-    F.zeta = A.get<float>(capf);
-    F.flagpass = A.get<int>(capf);
-    k.nbr_max = p->dim == 3 ? 64 : 32;  // a multiple of 4 (blocked layout)
-    F.nbr = A.get<int>((int64_t)k.nbr_max * capf);
-    F.nbr_cnt = A.get<unsigned int>(capf);
-    BoundBuf &B = c.B;
-    B.cap = capb;
-    B.count = A.get<int>(nn);
-    B.start = A.get<int>(nn + 1);
-    B.slot = A.get<int>(capb);
-    B.perm = A.get<int>(capb);
-    B.inv = A.get<int>(capb);
-    B.pos = A.get<float4>(capb);
-    B.mv = A.get<float2>(capb);
-    B.vadv = A.get<float4>(capb);
-    B.kappa = A.get<float>(capb);
-    B.W = A.get<float>(capb);
-    B.rho = A.get<float>(capb);
-    B.comp = A.get<float>(capb);
-    B.a2 = A.get<float>(capb);
-    B.alpha = A.get<float>(capb);
-    const int64_t nmax = capf > capb ? capf : capb;
-    c.S.partials_len = 8 * (int64_t)blocks_for(nmax) + 64;  // up to 8 threads per particle
-    c.S.partials = A.get<double>(c.S.partials_len);
-    const int64_t nscan = (nn + 4095) / 4096 + 1;
-    c.S.scan_len = 2 * nscan;
-    c.S.scan_blocks = A.get<int>(c.S.scan_len);
-    c.dp = A.get<DevPersist>(1);
-    c.ds = A.get<DevStep>(1);
-    if (A.err != cudaSuccess) {
-        int rc = fail_cuda(A.err, "cudaMalloc in tsph_create");
-        tsph_destroy(&c);
-        return rc;
+const char *tsph_last_error(void) { return g_last_error; }
+
+int tsph_create(const tsph_params *p, int64_t capf, int64_t capb, tsph_ctx **out) {
+    if (capf > 0x7fff0000ll || capb > 0x7fff0000ll) return fail(TSPH_ERR_INVALID, "capacity out of range");
+    return create_impl(p, 1, nullptr, nullptr, 0, capf, capb, out);
+}
+
+int tsph_create_batch(const tsph_params *scenes, int n_scenes, const int64_t *fluid_counts,
+                      const int64_t *bound_counts, tsph_ctx **out) {
+    if (!scenes || !fluid_counts || !bound_counts || n_scenes < 1)
+        return fail(TSPH_ERR_INVALID, "null argument or no scene");
+    long long tf = 0, tb = 0;
+    for (int s = 0; s < n_scenes; ++s) {
+        tf += fluid_counts[s];
+        tb += bound_counts[s];
     }
-    cudaError_t e = cudaMallocHost(&c.host_ds, sizeof(DevStep));
-    if (e == cudaSuccess) e = cudaMallocHost(&c.host_dp, sizeof(DevPersist));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&box->x.cap_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&box->x.body_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    if (e != cudaSuccess) {
-        int rc = fail_cuda(e, "tsph_create");
-        tsph_destroy(&c);
-        return rc;
-    }
-    c.use_graph = 1;
-    c.tpp = 1;
-    *out = &c;
-    return TSPH_OK;
+    if (tf > 0x7fff0000ll || tb > 0x7fff0000ll) return fail(TSPH_ERR_INVALID, "batch particle count out of range");
+    return create_impl(scenes, n_scenes, fluid_counts, bound_counts, 1, 0, 0, out);
 }
 
 int tsph_destroy(tsph_ctx *c) {
@@ -412,8 +544,7 @@ int tsph_destroy(tsph_ctx *c) {
     CtxBox *box = reinterpret_cast<CtxBox *>(c);
     if (c->exec) cudaGraphExecDestroy(c->exec);
     for (void *p : box->x.alloc.ptrs) cudaFree(p);
-    if (c->host_ds) cudaFreeHost(c->host_ds);
-    if (c->host_dp) cudaFreeHost(c->host_dp);
+    for (void *p : box->x.pinned) cudaFreeHost(p);
     if (box->x.cap_stream) cudaStreamDestroy(box->x.cap_stream);
     if (box->x.body_stream) cudaStreamDestroy(box->x.body_stream);
     delete box;
@@ -428,7 +559,8 @@ int tsph_set_graph_mode(tsph_ctx *c, int use_graph) {
 
 int tsph_set_threads_per_particle(tsph_ctx *c, int tpp) {
     if (!c) return fail(TSPH_ERR_INVALID, "null ctx");
-    if (tpp != 1 && tpp != 2 && tpp != 4 && tpp != 8) return fail(TSPH_ERR_INVALID, "threads per particle must be 1, 2, 4 or 8");
+    if (tpp != 1 && tpp != 2 && tpp != 4 && tpp != 8)
+        return fail(TSPH_ERR_INVALID, "threads per particle must be 1, 2, 4 or 8");
     if (tpp != c->tpp && c->exec) {
         cudaGraphExecDestroy(c->exec);
         c->exec = nullptr;
@@ -439,7 +571,9 @@ int tsph_set_threads_per_particle(tsph_ctx *c, int tpp) {
 
 int tsph_cfl_condition(tsph_ctx *c, const tsph_set *f, void *stream) {
     if (!c || !f) return fail(TSPH_ERR_INVALID, "null argument");
-    launch_cfl(*c, *f, (cudaStream_t)stream);
+    cudaStream_t st = (cudaStream_t)stream;
+    TSPH_CK(cudaMemsetAsync(c->k.dg->ticket, 0, sizeof(unsigned int), st));
+    launch_cfl(*c, *f, st);
     TSPH_CK(cudaGetLastError());
     return TSPH_OK;
 }
@@ -452,67 +586,54 @@ int tsph_substep(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream
     return run_step(c, f, b, stream, true);
 }
 
-int tsph_read_stats(tsph_ctx *c, tsph_stats *out, void *stream) {
-    if (!c || !out) return fail(TSPH_ERR_INVALID, "null argument");
+int tsph_read_scene_stats(tsph_ctx *c, int first, int count, tsph_stats *out, void *stream) {
+    if (!c || !out || first < 0 || count < 0 || first + count > c->n_scenes)
+        return fail(TSPH_ERR_INVALID, "bad scene range");
     cudaStream_t st = (cudaStream_t)stream;
-    TSPH_CK(cudaMemcpyAsync(c->host_ds, c->ds, sizeof(DevStep), cudaMemcpyDeviceToHost, st));
-    TSPH_CK(cudaMemcpyAsync(c->host_dp, c->dp, sizeof(DevPersist), cudaMemcpyDeviceToHost, st));
+    TSPH_CK(cudaMemcpyAsync(c->host_ss, c->k.ss, sizeof(SceneStep) * c->n_scenes, cudaMemcpyDeviceToHost, st));
+    TSPH_CK(cudaMemcpyAsync(c->host_sp, c->k.sp, sizeof(ScenePersist) * c->n_scenes, cudaMemcpyDeviceToHost, st));
     TSPH_CK(cudaStreamSynchronize(st));
-    const DevStep &s = *c->host_ds;
-    const DevPersist &d = *c->host_dp;
-    std::memset(out, 0, sizeof(*out));
-    out->dt = d.dt;
-    out->time_count = d.time_count;
-    out->compression = d.compression;
-    out->kinetic_energy = s.kinetic_energy;
-    out->potential_energy = s.potential_energy;
-    out->div_iter = s.div_iter;
-    out->incom_iter = s.incom_iter;
-    out->fbm_passes = s.fbm_passes;
-    out->general_flag = c->p.fbm_enabled ? s.gflag_out : 1;
-    out->status = s.status;
-    out->fluid_in_grid = -1;
-    out->bound_in_grid = -1;
-    out->steps = c->stepped;
-    out->total_div_iter = d.total_div_iter;
-    out->total_incom_iter = d.total_incom_iter;
-    out->total_fbm_passes = d.total_fbm_passes;
-    out->max_dens_compression = d.max_dens_compression;
-    out->launches_per_step = c->launches_per_step;
-    out->launches_per_iter = 2;
-    out->launches_per_pass = 1;
+    for (int i = 0; i < count; ++i) fill_stats(c, first + i, out + i);
     return TSPH_OK;
 }
 
+int tsph_read_stats(tsph_ctx *c, tsph_stats *out, void *stream) {
+    return tsph_read_scene_stats(c, 0, 1, out, stream);
+}
+
 int tsph_profile_phases(tsph_ctx *c, const tsph_set *f, const tsph_set *b, int reps, float *ms_out, void *stream) {
-    if (!c || !f || !b || !ms_out || reps < 1) return fail(TSPH_ERR_INVALID, "bad argument");
-    if (f->n > c->F.cap || b->n > c->B.cap) return fail(TSPH_ERR_CAPACITY, "part_num above capacity");
+    if (!ms_out || reps < 1) return fail(TSPH_ERR_INVALID, "bad argument");
+    int rc = bind_sets(c, f, b);
+    if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    const int S = c->n_scenes;
     // keep the persistent scalars (clock, counters) as they were
-    TSPH_CK(cudaMemcpyAsync(c->host_dp, c->dp, sizeof(DevPersist), cudaMemcpyDeviceToHost, st));
+    std::vector<ScenePersist> saved(S);
+    TSPH_CK(cudaMemcpyAsync(saved.data(), c->k.sp, sizeof(ScenePersist) * S, cudaMemcpyDeviceToHost, st));
     TSPH_CK(cudaStreamSynchronize(st));
-    const DevPersist saved = *c->host_dp;
     cudaEvent_t e0, e1;
     TSPH_CK(cudaEventCreate(&e0));
     TSPH_CK(cudaEventCreate(&e1));
-    const int64_t nf = f->n, nb = b->n;
     for (int ph = 0; ph < TSPH_PH_COUNT; ++ph) {
-        // state every phase expects: a fresh step through the density sweep
+        // state every phase expects: a fresh step through the first Jacobi sweep
         launch_step_begin(*c, st);
         launch_cfl(*c, *f, st);
         launch_grid_build(*c, *f, *b, st);
-        launch_density(*c, nf, nb, st);
+        launch_density(*c, st);
         launch_solve_begin(*c, kSolveDiv, 0, 0, st);
-        if (nf > 0) launch_psi(*c, nf, st);
+        launch_psi(*c, st);
         TSPH_CK(cudaEventRecord(e0, st));
         for (int r = 0; r < reps; ++r) {
             switch (ph) {
                 case TSPH_PH_CFL: launch_cfl(*c, *f, st); break;
                 case TSPH_PH_GRID: launch_grid_build(*c, *f, *b, st); break;
-                case TSPH_PH_DENSITY: launch_density(*c, nf, nb, st); break;
-                case TSPH_PH_PSI: if (nf > 0) launch_psi(*c, nf, st); break;
-                case TSPH_PH_VEL: if (nf > 0) launch_vel(*c, nf, kSolveDiv, 0, 0, st); break;
-                case TSPH_PH_ADVECT: launch_advect(*c, nf, st); break;
+                case TSPH_PH_DENSITY: launch_density(*c, st); break;
+                case TSPH_PH_PSI: launch_psi(*c, st); break;
+                case TSPH_PH_VEL:
+                    launch_solve_begin(*c, kSolveDiv, 0, 0, st);  // keep every scene running
+                    launch_vel(*c, kSolveDiv, 0, 0, st);
+                    break;
+                case TSPH_PH_ADVECT: launch_advect(*c, st); break;
                 case TSPH_PH_UNSORT: launch_unsort(*c, *f, *b, st); break;
             }
         }
@@ -524,8 +645,7 @@ int tsph_profile_phases(tsph_ctx *c, const tsph_set *f, const tsph_set *b, int r
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    *c->host_dp = saved;
-    TSPH_CK(cudaMemcpyAsync(c->dp, c->host_dp, sizeof(DevPersist), cudaMemcpyHostToDevice, st));
+    TSPH_CK(cudaMemcpyAsync(c->k.sp, saved.data(), sizeof(ScenePersist) * S, cudaMemcpyHostToDevice, st));
     TSPH_CK(cudaStreamSynchronize(st));
     TSPH_CK(cudaGetLastError());
     return TSPH_OK;
@@ -533,19 +653,19 @@ int tsph_profile_phases(tsph_ctx *c, const tsph_set *f, const tsph_set *b, int r
 
 int tsph_set_state(tsph_ctx *c, double time_count, float dt, double compression, void *stream) {
     if (!c) return fail(TSPH_ERR_INVALID, "null ctx");
-    k_set_state<<<1, 1, 0, (cudaStream_t)stream>>>(c->dp, time_count, dt, compression);
+    k_set_state<<<(c->n_scenes + 127) / 128, 128, 0, (cudaStream_t)stream>>>(c->k, time_count, dt, compression);
     TSPH_CK(cudaGetLastError());
     return TSPH_OK;
 }
 
 int tsph_neighbor_stats(tsph_ctx *c, const tsph_set *f, const tsph_set *b, int32_t *fc, uint64_t *fh, int32_t *bc,
                         uint64_t *bh, void *stream) {
-    if (!c || !f || !b) return fail(TSPH_ERR_INVALID, "null argument");
-    if (f->n > c->F.cap || b->n > c->B.cap) return fail(TSPH_ERR_CAPACITY, "part_num above capacity");
+    int rc = bind_sets(c, f, b);
+    if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     launch_step_begin(*c, st);
     launch_grid_build(*c, *f, *b, st);
-    launch_neighbor_stats(*c, f->n, b->n, fc, fh, bc, bh, st);
+    launch_neighbor_stats(*c, fc, fh, bc, bh, st);
     TSPH_CK(cudaGetLastError());
     TSPH_CK(cudaStreamSynchronize(st));
     return TSPH_OK;

@@ -1,16 +1,22 @@
 // Internal definitions shared by the CUDA translation units of the SPH hot path.
 //
-// Data layout (all in HBM, owned by tsph_ctx):
-//   * two cell grids (fluid, boundary) over the reference's linear cell codes
-//     code = x + nx*y + nx*ny*z (sph_config.py:210-214): count[node_num] and the
-//     exclusive scan start[node_num + 1];
-//   * per set, a permutation perm[sorted slot] = particle id, sorted by cell code
-//     with ties broken by particle id; particles without a valid cell sit after
-//     the in-grid ones (they still run their own sums, sph.py:52, but are never
-//     found as neighbours, sph_obj.py:305,319);
+// A context steps one scene (the reference's drop-in case) or a batch of
+// independent scenes in the same launches.  Data layout (all in HBM, owned by
+// tsph_ctx):
+//   * scene s owns the cell codes [cbase_s, cbase_s + node_num_s) of one global
+//     code space (segmented grids); inside a scene a code is the reference's
+//     linear x + nx*y + nx*ny*z (sph_config.py:210-214).  Two grids (fluid,
+//     boundary): count[total_nodes] and the exclusive scan start[total_nodes+1];
+//   * per set, a permutation perm[sorted slot] = particle id.  Scene s's sorted
+//     slots are [slot_s, slot_s + slots_s), a multiple of kChunk, so no block of
+//     256 threads ever straddles two scenes: first its in-grid particles by cell
+//     code, ties by particle id, then its particles without a valid cell (they
+//     still run their own sums, sph.py:52, but are never found as neighbours,
+//     sph_obj.py:305,319), then padding slots that no kernel processes;
 //   * sorted SoA copies of the per-particle state as float4 (x, y, z, X) etc., so
 //     a neighbour cell row (three x-adjacent cells) is one contiguous, coalesced
-//     range of 16-byte loads.
+//     range of 16-byte loads;
+//   * per-scene constants, persistent scalars and per-step scalars.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -21,49 +27,98 @@
 namespace tsph {
 
 constexpr int kBlock = 256;     // threads per block of the particle sweeps
+constexpr int kChunk = 256;     // a scene's sorted slots are padded to multiples of this
 constexpr int kMaxP = TSPH_MAX_PHASES;
 
-// Scalars that persist across steps (device resident).
-struct DevPersist {
-    double time_count;
-    double compression;  // carried into the next divergence-loop test (main.py:201)
-    float dt;
-    int32_t steps;
-    long long total_div_iter, total_incom_iter, total_fbm_passes;
-    double max_dens_compression;
-};
-
-// Scalars of one step; zeroed by a memset at the start of every step.
-struct DevStep {
-    unsigned int vmax_bits;     // max |v| over fluid (float bits, non-negative)
-    int32_t cur;                // which v_adv buffer is current
-    int32_t iter;               // iteration counter of the running solve
-    int32_t cond;               // loop condition (mirrors the graph conditional)
-    int32_t div_iter, incom_iter;
-    int32_t fbm_pass, general_flag, fbm_passes, fbm_cond;
-    int32_t f_tail, b_tail;     // particles without a valid cell
-    int32_t status;
-    int32_t gflag_out;          // general_flag after the last volume-fraction pass
-    unsigned int ticket[8];
-    double kinetic_energy, potential_energy;
-    double psi_sum;             // sum of psi_adv / psi0 of the last Jacobi sweep A
-};
-
-// Launch-time constants of one context (passed by value: lands in the constant bank).
-struct KConst {
+// Constants of one scene (the reference's Config, sph_config.py:83-235, in f32)
+// and its particle segments.
+struct SceneConst {
     float lb[3];
-    float h, h2, inv_h, sig, sig_h;   // sig_h = sig / h
-    long long node_num, nx, nxny;
-    int R;                            // neighb_range
-    int dim, P, vfsph;
+    float h, h2, inv_h, sig, sig_h, c_coh;   // c_coh = 32 / (pi h^3)
+    long long node_num, nx, nxny, cbase;
     float g[3];
     float mu, gamma, fbm_c, fbm_D;
     float rho_phase[kMaxP];
     float part_size, cfl;
     int cs, iter_min, iter_max, fbm_max_passes;
     float div_tol, comp_tol;
-    float c_coh;                      // 32 / (pi h^3), cohesion normaliser
-    int nbr_max;                      // neighbour-list slots per fluid particle
+    // caller order [f_user, f_user + f_n); sorted slots [f_slot, f_slot + f_slots)
+    long long f_user, f_n, f_slot, f_slots;
+    long long b_user, b_n, b_slot, b_slots;
+};
+
+// Scalars of a scene that persist across steps.
+struct ScenePersist {
+    double time_count;
+    double compression;  // carried into the next divergence-loop test (main.py:201)
+    double max_dens_compression;
+    long long total_div_iter, total_incom_iter, total_fbm_passes;
+    float dt;
+    int32_t steps;
+};
+
+// Scalars of a scene for one step; zeroed at the start of every step.
+struct SceneStep {
+    unsigned int vmax_bits;     // max |v| over the scene's fluid (float bits)
+    int32_t cur;                // which v_adv buffer is current
+    int32_t iter, cond;         // running solve: iteration counter, loop condition
+    int32_t div_iter, incom_iter;
+    int32_t fbm_pass, general_flag, fbm_passes, fbm_cond, gflag_out;
+    int32_t status;
+    int32_t f_tail, b_tail;     // particles without a valid cell
+    int32_t f_in, b_in;         // particles in the grid
+    long long f_shift, b_shift; // sorted slot of global scan position p is p + shift
+    unsigned int ticket[6];     // block tickets of this scene (psi, vel, fbm, update)
+    double psi_sum, kinetic_energy, potential_energy;
+};
+
+// Grid-wide scalars of one step; zeroed at the start of every step.
+struct DevGlobal {
+    unsigned int ticket[8];
+    int32_t cond_any, fbm_any, status;
+    int32_t pad;
+};
+
+enum GlobalTicket { kGtCfl = 0, kGtVel = 1, kGtFbm = 2, kGtUpdate = 3 };
+enum SceneTicket { kStPsi = 0, kStVel = 1, kStFbm = 2, kStUpdate = 3 };
+
+// Launch-time constants of one context (passed by value: the constant bank).
+struct KConst {
+    int dim, P, vfsph, R, nbr_max, n_scenes;
+    long long total_nodes;
+    long long f_slots, b_slots;           // padded slots over all scenes
+    const SceneConst *sc;
+    ScenePersist *sp;
+    SceneStep *ss;
+    DevGlobal *dg;
+    const int *f_chunk_scene;             // scene of each kChunk-slot chunk (fluid / boundary)
+    const int *b_chunk_scene;
+    const int *f_user_scene;              // scene of each caller-order particle
+    const int *b_user_scene;
+    const long long *cbase_list;          // cbase of every scene, then total_nodes
+};
+
+// The geometric constants a neighbour loop needs, in registers.
+struct Geo {
+    float lb[3];
+    float h, h2, inv_h, sig, sig_h;
+    long long node_num, nx, nxny, cbase;
+    int R;
+    __device__ __forceinline__ void load(const SceneConst &c, int R_) {
+        lb[0] = c.lb[0];
+        lb[1] = c.lb[1];
+        lb[2] = c.lb[2];
+        h = c.h;
+        h2 = c.h2;
+        inv_h = c.inv_h;
+        sig = c.sig;
+        sig_h = c.sig_h;
+        node_num = c.node_num;
+        nx = c.nx;
+        nxny = c.nxny;
+        cbase = c.cbase;
+        R = R_;
+    }
 };
 
 // nbr_cnt value of a particle whose neighbours did not fit the list: its sweeps
@@ -76,7 +131,7 @@ __host__ __device__ __forceinline__ int64_t nbr_index(int t, int64_t s, int64_t 
 }
 
 struct FluidBuf {
-    int64_t cap;
+    int64_t cap;             // padded slots over all scenes
     int *count, *start, *slot, *perm, *inv;
     float4 *pos;       // x, y, z, X (mass for DFSPH, rest_volume for VFSPH)
     float2 *mv;        // mass, rest_volume
@@ -138,51 +193,54 @@ __device__ __forceinline__ float kcoh(float q) {
     return q <= 0.5f ? 2.f * t - 1.f / 64.f : (q < 1.f ? t : 0.f);
 }
 
-// Cell of a position: floor((p - lb) / h) per axis with IEEE division
-// (sph_util.py:65-67), and the linear code (sph_util.py:70-72).  `ok` is false for
-// a non-finite position or a coordinate beyond +-2^40 cells.
+// Cell of a position inside its scene: floor((p - lb) / h) per axis with IEEE
+// division (sph_util.py:65-67), and the scene-local linear code
+// (sph_util.py:70-72).  `ok` is false for a non-finite position or a coordinate
+// beyond +-1e12 cells.
 template <int DIM>
-__device__ __forceinline__ long long cell_code(float4 p, const KConst &k, bool &ok) {
+__device__ __forceinline__ long long cell_code(float4 p, const Geo &g, bool &ok) {
     const float c[3] = {p.x, p.y, p.z};
     long long s[3] = {0, 0, 0};
     ok = true;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        float f = floorf(__fdiv_rn(c[d] - k.lb[d], k.h));
+        float f = floorf(__fdiv_rn(c[d] - g.lb[d], g.h));
         if (!(f > -1.0e12f && f < 1.0e12f)) ok = false;
         s[d] = ok ? (long long)f : 0;
     }
-    long long code = s[0] + s[1] * k.nx;
-    if (DIM == 3) code += s[2] * k.nxny;
+    long long code = s[0] + s[1] * g.nx;
+    if (DIM == 3) code += s[2] * g.nxny;
     return code;
 }
 
 // Visits every candidate the reference's template loop visits (sph.py:52-60):
 // for each row offset (dy, dz) the x-adjacent codes [rc - R, rc + R] clipped to
-// the valid range (0, node_num) form one contiguous range of sorted slots.
-// Codes are linear, so an x offset past a row end continues into the next row
-// exactly like dim_encode without bounds checks.
-template <int DIM, class F>
-__device__ __forceinline__ void visit_candidates(const int *__restrict__ start, const KConst &k,
-                                                 long long code, F &&f) {
-    const int R = k.R;
+// the scene's valid range (0, node_num) form one contiguous range of sorted
+// slots.  Codes are linear, so an x offset past a row end continues into the
+// next row exactly like dim_encode without bounds checks.  `shift` maps a scan
+// position of the grid to a sorted slot.  Lane q of a TPP-lane group visits only
+// j = beg + q, beg + q + TPP, ...
+template <int DIM, int TPP = 1, class F>
+__device__ __forceinline__ void visit_candidates(const int *__restrict__ start, const Geo &g, long long code,
+                                                 long long shift, int q, F &&f) {
+    const int R = g.R;
     const int zr = (DIM == 3) ? R : 0;
     for (int dz = -zr; dz <= zr; ++dz) {
         for (int dy = -R; dy <= R; ++dy) {
-            long long rc = code + dy * k.nx + dz * k.nxny;
+            long long rc = code + dy * g.nx + dz * g.nxny;
             long long lo = rc - R, hi = rc + R;
             if (lo < 1) lo = 1;
-            if (hi > k.node_num - 1) hi = k.node_num - 1;
+            if (hi > g.node_num - 1) hi = g.node_num - 1;
             if (lo > hi) continue;
-            const int beg = __ldg(start + lo);
-            const int end = __ldg(start + hi + 1);
-            for (int j = beg; j < end; ++j) f(j);
+            const int beg = (int)(__ldg(start + g.cbase + lo) + shift);
+            const int end = (int)(__ldg(start + g.cbase + hi + 1) + shift);
+            for (int j = beg + q; j < end; j += TPP) f(j);
         }
     }
 }
 
 // ---------------------------------------------------------------------------------
-// Deterministic block reduction in FP64 (warp shuffles, fixed tree).
+// Deterministic reductions in FP64 (warp shuffles, fixed trees).
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -204,28 +262,20 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
     return r;  // valid in thread 0
 }
 
-// True (in every thread) for the block that finishes last; the caller's per-block
-// results must already be stored.  Classic fence + ticket pattern: no thread ever
-// waits on another block.
-__device__ __forceinline__ bool last_block_done(unsigned int *ticket) {
+// True (in every thread) for the block that finishes last among `total`
+// arrivals on `ticket`; the caller's per-block results must already be stored.
+// Fence + ticket: no thread ever waits on another block.
+__device__ __forceinline__ bool last_block_done(unsigned int *ticket, unsigned int total) {
     __shared__ bool am_last;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned int t = atomicAdd(ticket, 1u);
-        am_last = (t == gridDim.x - 1);
+        am_last = (t == total - 1);
     }
     __syncthreads();
     if (am_last) __threadfence();
     return am_last;
-}
-
-// Sums partials[0..n) in a fixed order within one block (result in thread 0).
-template <int BS>
-__device__ __forceinline__ double sum_partials(const double *partials, int n, double *sh) {
-    double v = 0.0;
-    for (int i = threadIdx.x; i < n; i += BS) v += __ldcg(partials + i);
-    return block_sum<BS>(v, sh);
 }
 
 // Per-block FP64 sum without a block-wide barrier at the end (warps finish at
@@ -253,7 +303,7 @@ __device__ __forceinline__ bool block_sum_last_warp(double v, double *sh, unsign
     return true;
 }
 
-// Grid-wide version for one warp: true (in all its lanes) for the warp that
+// One-warp version of the grid ticket: true (in all its lanes) for the warp that
 // arrives last among `total` arriving warps.
 __device__ __forceinline__ bool last_warp_done(unsigned int *ticket, unsigned int total) {
     const int lane = threadIdx.x & 31;
@@ -268,29 +318,8 @@ __device__ __forceinline__ bool last_warp_done(unsigned int *ticket, unsigned in
     return last;
 }
 
-// Like visit_candidates, but lane q of a TPP-lane particle group visits only the
-// candidates j = beg + q, beg + q + TPP, ... of every row.
-template <int DIM, int TPP, class F>
-__device__ __forceinline__ void visit_candidates_strided(const int *__restrict__ start, const KConst &k,
-                                                         long long code, int q, F &&f) {
-    const int R = k.R;
-    const int zr = (DIM == 3) ? R : 0;
-    for (int dz = -zr; dz <= zr; ++dz) {
-        for (int dy = -R; dy <= R; ++dy) {
-            long long rc = code + dy * k.nx + dz * k.nxny;
-            long long lo = rc - R, hi = rc + R;
-            if (lo < 1) lo = 1;
-            if (hi > k.node_num - 1) hi = k.node_num - 1;
-            if (lo > hi) continue;
-            const int beg = __ldg(start + lo);
-            const int end = __ldg(start + hi + 1);
-            for (int j = beg + q; j < end; j += TPP) f(j);
-        }
-    }
-}
-
 // Lane layout of a sweep with TPP threads per particle: a warp serves 32 / TPP
-// consecutive particles; lane = q * (32 / TPP) + p handles particle p of the warp
+// consecutive sorted slots; lane = q * (32 / TPP) + p handles slot p of the warp
 // and every TPP-th four-entry block of its neighbour list starting at block q, so
 // lanes with the same q read one contiguous 16 * 32 / TPP-byte run of the list.
 template <int TPP>
@@ -350,20 +379,32 @@ __device__ __forceinline__ void walk_blocks(const int *__restrict__ nbr, int64_t
 // selected; the callbacks keep their own 0 < r < h test, which is what selects
 // the pairs on the scanning path.
 template <int DIM, bool BOUND, int TPP, class FF, class FB>
-__device__ __forceinline__ void for_each_neighbor_tpp(const KConst &k, const FluidBuf &F, const BoundBuf &B,
-                                                      int64_t s, int q, float4 pi, FF &&ff, FB &&fb) {
+__device__ __forceinline__ void for_each_neighbor_tpp(const Geo &g, const FluidBuf &F, const BoundBuf &B,
+                                                      long long f_shift, long long b_shift, int64_t s, int q,
+                                                      float4 pi, FF &&ff, FB &&fb) {
     const unsigned int pc = F.nbr_cnt[s];
     if (pc != kNbrOverflow) {
         const int nfl = (int)(pc & 0xffffu), nbo = (int)(pc >> 16);
         walk_blocks<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl, ff, fb);
     } else {
         bool ok;
-        const long long code = cell_code<DIM>(pi, k, ok);
+        const long long code = cell_code<DIM>(pi, g, ok);
         if (ok) {
-            visit_candidates_strided<DIM, TPP>(F.start, k, code, q, ff);
-            if (BOUND) visit_candidates_strided<DIM, TPP>(B.start, k, code, q, fb);
+            visit_candidates<DIM, TPP>(F.start, g, code, f_shift, q, ff);
+            if (BOUND) visit_candidates<DIM, TPP>(B.start, g, code, b_shift, q, fb);
         }
     }
+}
+
+// Scene of a global cell code (binary search over the scenes' cbase list).
+__device__ __forceinline__ int scene_of_cell(const KConst &k, long long code) {
+    int lo = 0, hi = k.n_scenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (k.cbase_list[mid] <= code) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 inline int blocks_for(int64_t n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }

@@ -6,24 +6,26 @@
 #include "common.cuh"
 
 struct tsph_ctx {
-    tsph_params p;
+    tsph_params p;            // parameters of scene 0 (features shared by every scene)
     tsph::KConst k;
     tsph::FluidBuf F;
     tsph::BoundBuf B;
     tsph::Scratch S;
-    tsph::DevPersist *dp;
-    tsph::DevStep *ds;
-    tsph::DevStep *host_ds;    // pinned mirror for host-loop mode and stats
-    tsph::DevPersist *host_dp;
+    tsph::SceneConst *host_sc;  // host copy of the scene table (pinned)
+    tsph::SceneStep *host_ss;   // pinned mirrors for host-loop mode and stats
+    tsph::ScenePersist *host_sp;
+    tsph::DevGlobal *host_dg;
+    int n_scenes;
+    int batch;                // 0: one scene whose particle counts follow the caller's sets
+    int st_on;                // some scene has surface tension
     int use_graph;
     int stepped;
     // cached per-substep graph, keyed on the particle counts and array pointers
     cudaGraphExec_t exec;
     unsigned long long graph_key[4];
-    int graph_substep;         // whether the cached graph includes cfl_condition
-    int launches;              // kernel launches enqueued (counted by the launchers)
-    int launches_per_step;     // top-level kernels of the last enqueued step
-    int tpp;                   // threads per particle of the list sweeps (1, 2, 4, 8)
+    int launches;             // kernel launches enqueued (counted by the launchers)
+    int launches_per_step;    // top-level kernels of the last enqueued step
+    int tpp;                  // threads per particle of the list sweeps (1, 2, 4, 8)
 };
 
 namespace tsph {
@@ -35,24 +37,18 @@ void launch_step_begin(tsph_ctx &c, cudaStream_t st);
 void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st);
 void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);
 void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);
-void launch_neighbor_stats(tsph_ctx &c, int64_t nf, int64_t nb, int32_t *fc, uint64_t *fh,
-                           int32_t *bc, uint64_t *bh, cudaStream_t st);
+void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, uint64_t *bh, cudaStream_t st);
 
 // sweeps.cu
-void launch_density(tsph_ctx &c, int64_t nf, int64_t nb, cudaStream_t st);
-void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond,
-                        cudaStream_t st);
-void launch_solve_iter(tsph_ctx &c, int64_t nf, int kind, cudaGraphConditionalHandle h,
-                       int use_cond, cudaStream_t st);
-void launch_psi(tsph_ctx &c, int64_t nf, cudaStream_t st);
-void launch_vel(tsph_ctx &c, int64_t nf, int kind, cudaGraphConditionalHandle h, int use_cond,
-                cudaStream_t st);
-void launch_advect(tsph_ctx &c, int64_t nf, cudaStream_t st);
+void launch_density(tsph_ctx &c, cudaStream_t st);
+void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
+void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
+void launch_psi(tsph_ctx &c, cudaStream_t st);
+void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
+void launch_advect(tsph_ctx &c, cudaStream_t st);
 
 // fbm.cu
-void launch_fbm_begin(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond,
-                      cudaStream_t st);
-void launch_fbm_pass(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond,
-                     cudaStream_t st);
+void launch_fbm_begin(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
+void launch_fbm_pass(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
 
 }  // namespace tsph

@@ -10,30 +10,47 @@
 // convective and diffusive flux of each unflagged particle over its unflagged
 // neighbours and flags it if any phase would go negative; flags set during pass
 // p (value p) do not exclude a neighbour until pass p + 1, which is what the
-// reference's separate check kernel achieves.  The number of passes is capped
-// (fbm_max_passes); the reference loops forever if a flagged particle's own
-// volume fraction is already negative.
+// reference's separate check kernel achieves.  Each scene runs its own pass
+// loop; the graph loop runs while any scene does.  The number of passes is
+// capped (fbm_max_passes); the reference loops forever if a flagged particle's
+// own volume fraction is already negative.
 #include <cuda_runtime.h>
 
 #include "ctx.h"
 
 namespace tsph {
 
-__global__ void k_fbm_begin(DevStep *ds, cudaGraphConditionalHandle h, int use_cond) {
-    ds->fbm_pass = 0;
-    ds->general_flag = 0;
-    ds->fbm_cond = 1;  // SPH_clean_value sets general_flag = 1: at least one pass
-    if (use_cond) cudaGraphSetConditional(h, 1u);
+__global__ void k_fbm_begin(KConst k, cudaGraphConditionalHandle h, int use_cond) {
+    __shared__ int any_sh;
+    if (threadIdx.x == 0) any_sh = 0;
+    __syncthreads();
+    int any = 0;
+    for (int s = threadIdx.x; s < k.n_scenes; s += blockDim.x) {
+        SceneStep &st = k.ss[s];
+        st.fbm_pass = 0;
+        st.general_flag = 0;
+        // SPH_clean_value sets general_flag = 1: at least one pass
+        st.fbm_cond = k.sc[s].f_n > 0 ? 1 : 0;
+        st.gflag_out = st.fbm_cond;
+        any |= st.fbm_cond;
+    }
+    if (any) atomicOr(&any_sh, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        k.dg->fbm_any = any_sh;
+        if (use_cond) cudaGraphSetConditional(h, any_sh ? 1u : 0u);
+    }
 }
 
 // First loop of SPH_FBM_convect, sph.py:331-345.
 template <int DIM, int P>
-__global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F, int64_t n, const DevStep *ds,
-                                                      const DevPersist *dp) {
+__global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= n) return;
-    const float dt = dp->dt;
-    const float4 va = F.vadv[ds->cur * F.cap + s];
+    const int sc = k.f_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
+    const SceneConst &c = k.sc[sc];
+    if (s - c.f_slot >= c.f_n) return;
+    const float dt = k.sp[sc].dt;
+    const float4 va = F.vadv[k.ss[sc].cur * F.cap + s];
     const float4 v = F.vel[s];
     const float ax = (va.x - v.x) / dt, ay = (va.y - v.y) / dt, az = (va.z - v.z) / dt;
     const float rho0 = F.rho0[s];
@@ -42,17 +59,17 @@ __global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F, int6
 #pragma unroll
     for (int q = 0; q < P; ++q) {
         vf[q] = F.vf[q * F.cap + s];
-        zeta += vf[q] * (k.rho_phase[q] - rho0) / k.rho_phase[q];
+        zeta += vf[q] * (c.rho_phase[q] - rho0) / c.rho_phase[q];
     }
-    const float gz = DIM == 3 ? k.g[2] : 0.f;
-    const float fx = (ax - zeta * k.g[0]) / (1.f - zeta);
-    const float fy = (ay - zeta * k.g[1]) / (1.f - zeta);
+    const float gz = DIM == 3 ? c.g[2] : 0.f;
+    const float fx = (ax - zeta * c.g[0]) / (1.f - zeta);
+    const float fy = (ay - zeta * c.g[1]) / (1.f - zeta);
     const float fz = (az - zeta * gz) / (1.f - zeta);
 #pragma unroll
     for (int q = 0; q < P; ++q) {
-        const float c = vf[q] * (k.rho_phase[q] - rho0);
-        float dx = c * (k.g[0] - fx), dy = c * (k.g[1] - fy), dz = c * (gz - fz);
-        const float w = vf[q] * k.rho_phase[q];
+        const float cq = vf[q] * (c.rho_phase[q] - rho0);
+        float dx = cq * (c.g[0] - fx), dy = cq * (c.g[1] - fy), dz = cq * (gz - fz);
+        const float w = vf[q] * c.rho_phase[q];
         if (w > 1e-6f) {
             dx /= w; dy /= w; dz /= w;
         } else {
@@ -67,17 +84,21 @@ __global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F, int6
 }
 
 // One pass: SPH_FBM_clean_tmp + pair loop of SPH_FBM_convect + SPH_FBM_diffuse +
-// SPH_FBM_check_tmp (sph.py:301-372).  The last block evaluates the loop test.
+// SPH_FBM_check_tmp (sph.py:301-372).  The scene's last block evaluates its loop
+// test; the grid's last block sets the graph condition.
 template <int DIM, int P>
-__global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, int64_t n, DevStep *ds,
-                                                     const DevPersist *dp, cudaGraphConditionalHandle h,
-                                                     int use_cond) {
+__global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, BoundBuf B,
+                                                     cudaGraphConditionalHandle h, int use_cond) {
     __shared__ int any_neg;
+    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    const int sc = k.f_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
+    const SceneConst &c = k.sc[sc];
+    SceneStep &st = k.ss[sc];
+    const bool running = st.fbm_cond != 0;
     if (threadIdx.x == 0) any_neg = 0;
     __syncthreads();
-    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    const int pass = ds->fbm_pass + 1;
-    if (s < n) {
+    const int pass = st.fbm_pass + 1;
+    if (running && s - c.f_slot < c.f_n) {
         const int fp = F.flagpass[s];
         float tmp[P];
         float vfi[P];
@@ -87,22 +108,24 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, int64
             vfi[q] = F.vf[q * F.cap + s];
         }
         if (fp == 0) {
-            const float dt = dp->dt;
+            Geo g;
+            g.load(c, k.R);
+            const float dt = k.sp[sc].dt;
             const float4 pi = F.pos[s];
             float4 ui[P];
 #pragma unroll
             for (int q = 0; q < P; ++q) ui[q] = F.drift[q * F.cap + s];
-            const float cc = k.fbm_c * dt, cd = dt * k.fbm_D, eps = 0.01f * k.h2;
-            for_each_neighbor_tpp<DIM, false, 1>(k, F, BoundBuf{}, s, 0, pi,
+            const float cc = c.fbm_c * dt, cd = dt * c.fbm_D, eps = 0.01f * g.h2;
+            for_each_neighbor_tpp<DIM, false, 1>(g, F, B, st.f_shift, st.b_shift, s, 0, pi,
                 [&](int j) {
                     const float4 pj = F.pos[j];
                     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                     const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (!(r2 < k.h2 && r2 > 0.f)) return;
+                    if (!(r2 < g.h2 && r2 > 0.f)) return;
                     const int fj = F.flagpass[j];
                     if (fj != 0 && fj != pass) return;
                     const float r = sqrtf(r2);
-                    const float wg = kwg(r * k.inv_h) * k.sig_h;
+                    const float wg = kwg(r * g.inv_h) * g.sig_h;
                     const float Vj = F.mv[j].y;
                     const float gx = dx / r * wg, gy = dy / r * wg, gz = dz / r * wg;
                     const float dif = cd * Vj * r * wg / (r2 + eps);
@@ -131,60 +154,73 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, int64
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0 && any_neg) atomicExch(&ds->general_flag, 1);
-    if (last_block_done(&ds->ticket[3])) {
-        if (threadIdx.x == 0) {
-            const int gf = atomicAdd(&ds->general_flag, 0);
-            ds->fbm_pass = pass;
-            ds->fbm_passes = pass;
-            ds->gflag_out = gf;
-            const int cond = gf && pass < k.fbm_max_passes;
-            if (gf && !cond) ds->status |= TSPH_ST_FBM_PASS_CAP;
-            ds->fbm_cond = cond;
-            ds->general_flag = 0;
-            ds->ticket[3] = 0;
-            if (use_cond) cudaGraphSetConditional(h, cond ? 1u : 0u);
+    if (running) {
+        if (threadIdx.x == 0 && any_neg) atomicExch(&st.general_flag, 1);
+        const unsigned int nblk = (unsigned int)(c.f_slots / kBlock);
+        if (last_block_done(&st.ticket[kStFbm], nblk)) {
+            if (threadIdx.x == 0) {
+                const int gf = atomicAdd(&st.general_flag, 0);
+                st.fbm_pass = pass;
+                st.fbm_passes = pass;
+                st.gflag_out = gf;
+                const int cond = gf && pass < c.fbm_max_passes;
+                if (gf && !cond) st.status |= TSPH_ST_FBM_PASS_CAP;
+                st.fbm_cond = cond;
+                st.general_flag = 0;
+                st.ticket[kStFbm] = 0;
+            }
+        }
+    }
+    if (last_block_done(&k.dg->ticket[kGtFbm], gridDim.x)) {
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            int any = 0;
+            for (int q = lane; q < k.n_scenes; q += 32) any |= (__ldcg(&k.ss[q].fbm_cond) != 0);
+            any = __any_sync(0xffffffffu, any);
+            if (lane == 0) {
+                k.dg->fbm_any = any;
+                k.dg->ticket[kGtFbm] = 0;
+                if (use_cond) cudaGraphSetConditional(h, any ? 1u : 0u);
+            }
         }
     }
 }
 
 template <int P>
-static void fbm_pass_dim(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st,
-                         bool drift) {
-    const int nb = blocks_for(nf) > 0 ? blocks_for(nf) : 1;
+static void fbm_pass_dim(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st, bool drift) {
+    const int nb = blocks_for(c.F.cap);
     if (c.k.dim == 3) {
-        if (drift) k_fbm_drift<3, P><<<nb, kBlock, 0, st>>>(c.k, c.F, nf, c.ds, c.dp);
-        else k_fbm_pass<3, P><<<nb, kBlock, 0, st>>>(c.k, c.F, nf, c.ds, c.dp, h, use_cond);
+        if (drift) k_fbm_drift<3, P><<<nb, kBlock, 0, st>>>(c.k, c.F);
+        else k_fbm_pass<3, P><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, h, use_cond);
     } else {
-        if (drift) k_fbm_drift<2, P><<<nb, kBlock, 0, st>>>(c.k, c.F, nf, c.ds, c.dp);
-        else k_fbm_pass<2, P><<<nb, kBlock, 0, st>>>(c.k, c.F, nf, c.ds, c.dp, h, use_cond);
+        if (drift) k_fbm_drift<2, P><<<nb, kBlock, 0, st>>>(c.k, c.F);
+        else k_fbm_pass<2, P><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, h, use_cond);
     }
 }
 
-static void fbm_dispatch(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st,
-                         bool drift) {
+static void fbm_dispatch(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st, bool drift) {
     switch (c.k.P) {
-        case 1: fbm_pass_dim<1>(c, nf, h, use_cond, st, drift); break;
-        case 2: fbm_pass_dim<2>(c, nf, h, use_cond, st, drift); break;
-        case 3: fbm_pass_dim<3>(c, nf, h, use_cond, st, drift); break;
-        case 4: fbm_pass_dim<4>(c, nf, h, use_cond, st, drift); break;
-        case 5: fbm_pass_dim<5>(c, nf, h, use_cond, st, drift); break;
-        case 6: fbm_pass_dim<6>(c, nf, h, use_cond, st, drift); break;
-        case 7: fbm_pass_dim<7>(c, nf, h, use_cond, st, drift); break;
-        default: fbm_pass_dim<8>(c, nf, h, use_cond, st, drift); break;
+        case 1: fbm_pass_dim<1>(c, h, use_cond, st, drift); break;
+        case 2: fbm_pass_dim<2>(c, h, use_cond, st, drift); break;
+        case 3: fbm_pass_dim<3>(c, h, use_cond, st, drift); break;
+        case 4: fbm_pass_dim<4>(c, h, use_cond, st, drift); break;
+        case 5: fbm_pass_dim<5>(c, h, use_cond, st, drift); break;
+        case 6: fbm_pass_dim<6>(c, h, use_cond, st, drift); break;
+        case 7: fbm_pass_dim<7>(c, h, use_cond, st, drift); break;
+        default: fbm_pass_dim<8>(c, h, use_cond, st, drift); break;
     }
 }
 
-void launch_fbm_begin(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
-    cudaMemsetAsync(c.F.flagpass, 0, sizeof(int) * (nf > 0 ? nf : 1), st);
-    c.launches += 1 + (nf > 0);
-    if (nf > 0) fbm_dispatch(c, nf, 0, 0, st, true);
-    k_fbm_begin<<<1, 1, 0, st>>>(c.ds, h, use_cond);
+void launch_fbm_begin(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+    cudaMemsetAsync(c.F.flagpass, 0, sizeof(int) * c.F.cap, st);
+    c.launches += 2;
+    fbm_dispatch(c, 0, 0, st, true);
+    k_fbm_begin<<<1, 256, 0, st>>>(c.k, h, use_cond);
 }
 
-void launch_fbm_pass(tsph_ctx &c, int64_t nf, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+void launch_fbm_pass(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
     c.launches += 1;
-    fbm_dispatch(c, nf, h, use_cond, st, false);
+    fbm_dispatch(c, h, use_cond, st, false);
 }
 
 }  // namespace tsph

@@ -1,5 +1,5 @@
 // Cell grid build (counting sort) and the gather / scatter between the caller's
-// particle order and the cell-sorted working order.
+// particle order and the cell-sorted working order, per scene.
 //
 // Reference: Ngrid.clear_node / encode / mem_shift / fill_node, sph_obj.py:295-323,
 // and the per-step bookkeeping of sph.py:22-47, 265-286.  Differences by design:
@@ -13,60 +13,78 @@
 namespace tsph {
 
 // ----------------------------------------------------------------------------- CFL
-// cfl_condition, sph.py:41-47: dt = part_size / cs, lowered to
+// cfl_condition, sph.py:41-47, per scene: dt = part_size / cs, lowered to
 // part_size / |v| * cfl_factor for |v| > 1e-4.  part_size / v * cfl is monotone
 // in v, so the minimum over particles is attained at max |v|.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_cfl(KConst k, const float *__restrict__ vel, int64_t n,
-                                                DevStep *ds, DevPersist *dp) {
-    float vmax = 0.f;
-    for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < n; i += (int64_t)gridDim.x * kBlock) {
-        float s = 0.f;
+__global__ void __launch_bounds__(kBlock) k_cfl(KConst k, const float *__restrict__ vel, int64_t n) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * kBlock;
+    for (int64_t base = blockIdx.x * (int64_t)kBlock; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        const bool act = i < n;
+        float vn = 0.f;
+        int sc = -1;
+        if (act) {
+            float s = 0.f;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            float v = vel[i * DIM + d];
-            s += v * v;
+            for (int d = 0; d < DIM; ++d) {
+                const float v = vel[i * DIM + d];
+                s += v * v;
+            }
+            vn = sqrtf(s);
+            if (!(vn > 1e-4f)) vn = 0.f;  // NaN norms fail the test, as in the reference
+            sc = k.f_user_scene[i];
         }
-        float vn = sqrtf(s);
-        if (vn > 1e-4f) vmax = fmaxf(vmax, vn);  // NaN norms fail the test, as in the reference
+        const int sc0 = __shfl_sync(0xffffffffu, sc, 0);
+        if (__all_sync(0xffffffffu, !act || sc == sc0)) {
+            float m = vn;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+            if (lane == 0 && m > 0.f) atomicMax(&k.ss[sc0].vmax_bits, __float_as_uint(m));
+        } else if (act && vn > 0.f) {
+            atomicMax(&k.ss[sc].vmax_bits, __float_as_uint(vn));
+        }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
-    if ((threadIdx.x & 31) == 0 && vmax > 0.f) atomicMax(&ds->vmax_bits, __float_as_uint(vmax));
-    if (last_block_done(&ds->ticket[0])) {
-        if (threadIdx.x == 0) {
-            float dt = __fdiv_rn(k.part_size, (float)k.cs);
-            float vm = __uint_as_float(atomicAdd(&ds->vmax_bits, 0u));
-            if (vm > 1e-4f) dt = fminf(dt, __fmul_rn(__fdiv_rn(k.part_size, vm), k.cfl));
-            dp->dt = dt;
-            dp->time_count += (double)dt;
-            ds->ticket[0] = 0;
+    if (last_block_done(&k.dg->ticket[kGtCfl], gridDim.x)) {
+        for (int s = threadIdx.x; s < k.n_scenes; s += kBlock) {
+            const SceneConst &c = k.sc[s];
+            float dt = __fdiv_rn(c.part_size, (float)c.cs);
+            const float vm = __uint_as_float(atomicExch(&k.ss[s].vmax_bits, 0u));
+            if (vm > 1e-4f) dt = fminf(dt, __fmul_rn(__fdiv_rn(c.part_size, vm), c.cfl));
+            k.sp[s].dt = dt;
+            k.sp[s].time_count += (double)dt;
         }
+        if (threadIdx.x == 0) k.dg->ticket[kGtCfl] = 0;
     }
 }
 
 // ----------------------------------------------------------------------------- encode
-// Ngrid.encode, sph_obj.py:300-306: structured cell, linear code, count.  A
-// particle without a valid code gets a slot in the tail (after all in-grid ones).
+// Ngrid.encode, sph_obj.py:300-306: structured cell, scene-local linear code,
+// count in the scene's range of the global grid.  A particle without a valid
+// code gets a rank in its scene's tail.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_encode(KConst k, tsph_set U, int *__restrict__ count,
-                                                   int *__restrict__ slot, int *tail, int *status) {
+__global__ void __launch_bounds__(kBlock) k_encode(KConst k, tsph_set U, int bound, int *__restrict__ count,
+                                                   int *__restrict__ slot) {
     const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (i >= U.n) return;
+    const int sc = bound ? k.b_user_scene[i] : k.f_user_scene[i];
+    Geo g;
+    g.load(k.sc[sc], k.R);
     float4 p = make_float4(U.pos[i * DIM], U.pos[i * DIM + 1], DIM == 3 ? U.pos[i * DIM + 2] : 0.f, 0.f);
     bool ok;
-    long long code = cell_code<DIM>(p, k, ok);
+    long long code = cell_code<DIM>(p, g, ok);
     const float c[3] = {p.x, p.y, p.z};
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
-        U.neighb_cell_structured_seq[i * DIM + d] = ok ? (int)floorf(__fdiv_rn(c[d] - k.lb[d], k.h)) : 0;
+        U.neighb_cell_structured_seq[i * DIM + d] = ok ? (int)floorf(__fdiv_rn(c[d] - g.lb[d], g.h)) : 0;
     U.neighb_cell_seq[i] = (int)code;
     int s;
-    if (ok && code > 0 && code < k.node_num) {
-        s = atomicAdd(count + code, 1);
+    if (ok && code > 0 && code < g.node_num) {
+        s = atomicAdd(count + g.cbase + code, 1);
     } else {
-        s = -1 - atomicAdd(tail, 1);
-        atomicOr(status, ok ? TSPH_ST_OUTSIDE_GRID : (TSPH_ST_NONFINITE_POS | TSPH_ST_OUTSIDE_GRID));
+        s = -1 - atomicAdd(bound ? &k.ss[sc].b_tail : &k.ss[sc].f_tail, 1);
+        atomicOr(&k.ss[sc].status, ok ? TSPH_ST_OUTSIDE_GRID : (TSPH_ST_NONFINITE_POS | TSPH_ST_OUTSIDE_GRID));
     }
     slot[i] = s;
 }
@@ -169,40 +187,43 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_add(ScanArgs a, int nbloc
     if (blockIdx.x == 0 && threadIdx.x == 0) a.start[g][a.n] = a.blocks[g][nblocks];
 }
 
-// ----------------------------------------------------------------------------- scatter
-struct ScatterArgs {
-    const int *code[2];
-    const int *slot[2];
-    const int *start[2];
-    int *perm[2];
-    int64_t n[2];
-    long long node_num;
-};
-
-__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs a) {
-    const int g = blockIdx.y;
-    const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (i >= a.n[g]) return;
-    const int sl = a.slot[g][i];
-    int s;
-    if (sl >= 0) s = a.start[g][a.code[g][i]] + sl;
-    else s = a.start[g][a.node_num] + (-1 - sl);
-    a.perm[g][s] = (int)i;
+// Per scene: in-grid counts and the shift from global scan positions to the
+// scene's sorted slots.
+__global__ void k_scene_shift(KConst k, const int *__restrict__ fstart, const int *__restrict__ bstart) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < k.n_scenes; s += gridDim.x * blockDim.x) {
+        const SceneConst &c = k.sc[s];
+        SceneStep &st = k.ss[s];
+        const int f0 = fstart[c.cbase], f1 = fstart[c.cbase + c.node_num];
+        const int b0 = bstart[c.cbase], b1 = bstart[c.cbase + c.node_num];
+        st.f_in = f1 - f0;
+        st.b_in = b1 - b0;
+        st.f_shift = c.f_slot - f0;
+        st.b_shift = c.b_slot - b0;
+    }
 }
 
-// Orders each cell's particles by id (insertion sort; cells hold ~2^dim..30).
-// Tail particles (no valid cell) are ordered too, by one thread per set.
-struct CellSortArgs {
-    const int *start[2];
-    int *perm[2];
-    int64_t n[2];
-    long long node_num;
-};
+// ----------------------------------------------------------------------------- scatter
+__global__ void __launch_bounds__(kBlock) k_scatter(KConst k, int bound, int64_t n, const int *__restrict__ code,
+                                                    const int *__restrict__ slot, const int *__restrict__ start,
+                                                    int *__restrict__ perm) {
+    const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (i >= n) return;
+    const int sc = bound ? k.b_user_scene[i] : k.f_user_scene[i];
+    const SceneConst &c = k.sc[sc];
+    const SceneStep &st = k.ss[sc];
+    const int sl = slot[i];
+    long long s;
+    if (sl >= 0) s = (long long)start[c.cbase + code[i]] + (bound ? st.b_shift : st.f_shift) + sl;
+    else s = (bound ? c.b_slot + st.b_in : c.f_slot + st.f_in) + (-1 - sl);
+    perm[s] = (int)i;
+}
 
-__device__ __forceinline__ void insertion_sort(int *p, int beg, int end) {
-    for (int a = beg + 1; a < end; ++a) {
+// Orders each cell's particles by id (insertion sort; cells hold ~2^dim..30),
+// blockIdx.y selecting the grid.
+__device__ __forceinline__ void insertion_sort(int *p, long long beg, long long end) {
+    for (long long a = beg + 1; a < end; ++a) {
         int v = p[a];
-        int b = a - 1;
+        long long b = a - 1;
         while (b >= beg && p[b] > v) {
             p[b + 1] = p[b];
             --b;
@@ -211,15 +232,27 @@ __device__ __forceinline__ void insertion_sort(int *p, int beg, int end) {
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_cell_sort(CellSortArgs a) {
+__global__ void __launch_bounds__(kBlock) k_cell_sort(KConst k, const int *__restrict__ fstart, int *fperm,
+                                                      const int *__restrict__ bstart, int *bperm) {
     const int g = blockIdx.y;
     const long long c = blockIdx.x * (long long)kBlock + threadIdx.x;
-    if (c < a.node_num) {
-        const int beg = a.start[g][c], end = a.start[g][c + 1];
-        if (end - beg > 1) insertion_sort(a.perm[g], beg, end);
-    } else if (c == a.node_num) {
-        insertion_sort(a.perm[g], a.start[g][a.node_num], (int)a.n[g]);
-    }
+    if (c >= k.total_nodes) return;
+    const int *start = g ? bstart : fstart;
+    const int beg = start[c], end = start[c + 1];
+    if (end - beg < 2) return;
+    const int sc = scene_of_cell(k, c);
+    const long long shift = g ? k.ss[sc].b_shift : k.ss[sc].f_shift;
+    insertion_sort(g ? bperm : fperm, beg + shift, end + shift);
+}
+
+// Each scene's particles without a valid cell, ordered by id (one thread per scene).
+__global__ void k_tail_sort(KConst k, int *fperm, int *bperm) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= k.n_scenes) return;
+    const SceneConst &c = k.sc[s];
+    const SceneStep &st = k.ss[s];
+    if (st.f_tail > 1) insertion_sort(fperm, c.f_slot + st.f_in, c.f_slot + st.f_in + st.f_tail);
+    if (st.b_tail > 1) insertion_sort(bperm, c.b_slot + st.b_in, c.b_slot + st.b_in + st.b_tail);
 }
 
 // ----------------------------------------------------------------------------- gather
@@ -229,7 +262,9 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(CellSortArgs a) {
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_gather_fluid(KConst k, tsph_set U, FluidBuf F) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= U.n) return;
+    if (s >= F.cap) return;
+    const SceneConst &c = k.sc[k.f_chunk_scene[s / kChunk]];
+    if (s - c.f_slot >= c.f_n) return;
     const int pid = F.perm[s];
     F.inv[pid] = (int)s;
     const float *p = U.pos + (int64_t)pid * DIM;
@@ -246,7 +281,9 @@ __global__ void __launch_bounds__(kBlock) k_gather_fluid(KConst k, tsph_set U, F
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= U.n) return;
+    if (s >= B.cap) return;
+    const SceneConst &c = k.sc[k.b_chunk_scene[s / kChunk]];
+    if (s - c.b_slot >= c.b_n) return;
     const int pid = B.perm[s];
     B.inv[pid] = (int)s;
     const float *p = U.pos + (int64_t)pid * DIM;
@@ -258,23 +295,25 @@ __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, B
     B.kappa[s] = U.psi_adv[pid];  // divided by alpha once alpha is known
 }
 
-// ----------------------------------------------------------------------------- unsort
-// Writes the step's results back in caller order, fused with SPH_update_volume_frac,
-// SPH_update_mass, SPH_update_pos and SPH_update_energy (sph.py:265-286, 375-379).
-// Energies: per-particle FP32 terms, FP64 block sums, fixed-order final sum.
+// ----------------------------------------------------------------------------- update
+// SPH_update_volume_frac, SPH_update_mass, SPH_update_pos and SPH_update_energy
+// (sph.py:265-286, 375-379) in sorted order, writing the step's results back to
+// the caller's particle order.  Energies: per-particle FP32 terms, FP64 block
+// sums, the scene's blocks summed in order by the scene's last block.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_unsort_fluid(KConst k, tsph_set U, FluidBuf F,
-                                                         const int *__restrict__ bstart, DevStep *ds,
-                                                         DevPersist *dp, double *partials,
-                                                         int fbm, int st_on) {
+__global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, FluidBuf F,
+                                                         const int *__restrict__ bstart, double *partials, int fbm,
+                                                         int st_on) {
     __shared__ double sh[kBlock / 32];
-    const int64_t pid = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    const int sc = k.f_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
+    const SceneConst &c = k.sc[sc];
+    SceneStep &st = k.ss[sc];
     double ke = 0.0, pe = 0.0;
-    if (pid < U.n) {
-        const int s = F.inv[pid];
-        const int cur = ds->cur;
-        const float dt = dp->dt;
-        const float4 v = F.vadv[cur * F.cap + s];
+    if (s - c.f_slot < c.f_n) {
+        const int pid = F.perm[s];
+        const float dt = k.sp[sc].dt;
+        const float4 v = F.vadv[st.cur * F.cap + s];
         const float4 p = F.pos[s];
         const float V = F.mv[s].y;
         const int flagged = fbm ? (F.flagpass[s] != 0) : 0;
@@ -284,10 +323,10 @@ __global__ void __launch_bounds__(kBlock) k_unsort_fluid(KConst k, tsph_set U, F
             if (fbm) {
                 const float t = F.vftmp[q * F.cap + s];
                 if (!flagged) vf += t;
-                U.volume_frac[pid * k.P + q] = vf;
-                U.volume_frac_tmp[pid * k.P + q] = t;
+                U.volume_frac[(int64_t)pid * k.P + q] = vf;
+                U.volume_frac_tmp[(int64_t)pid * k.P + q] = t;
             }
-            rho0 += k.rho_phase[q] * vf;
+            rho0 += c.rho_phase[q] * vf;
         }
         const float m = rho0 * V;
         const float np[3] = {p.x + v.x * dt, p.y + v.y * dt, p.z + v.z * dt};
@@ -298,25 +337,26 @@ __global__ void __launch_bounds__(kBlock) k_unsort_fluid(KConst k, tsph_set U, F
         const float a1v[3] = {a1.x, a1.y, a1.z};
         const float4 nr = F.normal[s];
         const float nrv[3] = {nr.x, nr.y, nr.z};
+        const int64_t b = (int64_t)pid * DIM;
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-            U.pos[pid * DIM + d] = np[d];
-            U.vel[pid * DIM + d] = vv[d];
-            U.vel_adv[pid * DIM + d] = vv[d];
-            U.acce_adv[pid * DIM + d] = aa[d];
-            U.alpha_1[pid * DIM + d] = a1v[d];
-            if (st_on) U.normal[pid * DIM + d] = nrv[d];
+            U.pos[b + d] = np[d];
+            U.vel[b + d] = vv[d];
+            U.vel_adv[b + d] = vv[d];
+            U.acce_adv[b + d] = aa[d];
+            U.alpha_1[b + d] = a1v[d];
+            if (st_on) U.normal[b + d] = nrv[d];
         }
         if (fbm) {
             const float4 fa = F.facc[s];
             const float fav[3] = {fa.x, fa.y, fa.z};
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) U.acce[pid * DIM + d] = fav[d];
+            for (int d = 0; d < DIM; ++d) U.acce[b + d] = fav[d];
             for (int q = 0; q < k.P; ++q) {
                 const float4 dv = F.drift[q * F.cap + s];
                 const float dvv[3] = {dv.x, dv.y, dv.z};
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) U.drift_vel[(pid * k.P + q) * DIM + d] = dvv[d];
+                for (int d = 0; d < DIM; ++d) U.drift_vel[((int64_t)pid * k.P + q) * DIM + d] = dvv[d];
             }
             U.fbm_zeta[pid] = F.zeta[s];
         }
@@ -329,53 +369,66 @@ __global__ void __launch_bounds__(kBlock) k_unsort_fluid(KConst k, tsph_set U, F
         U.psi_adv[pid] = F.psiadv[s];
         U.alpha[pid] = F.mpsi[s].w;
         U.alpha_2[pid] = F.a2[s];
-        const int code = U.neighb_cell_seq[pid];
-        if (code > 0 && code < k.node_num && s < F.start[k.node_num]) U.neighb_in_cell_seq[pid] = s + bstart[code];
+        if (s - c.f_slot < st.f_in) {
+            // slot in the reference's combined grid: cell offset over both sets, fluid first
+            const int code = U.neighb_cell_seq[pid];
+            U.neighb_in_cell_seq[pid] = (int)(s - st.f_shift) + bstart[c.cbase + code];
+        }
         float v2 = 0.f;
 #pragma unroll
         for (int d = 0; d < DIM; ++d) v2 += vv[d] * vv[d];
         ke = (double)(0.5f * m * v2);
-        pe = (double)(-m * k.g[1] * (np[1] - k.lb[1]));
+        pe = (double)(-m * c.g[1] * (np[1] - c.lb[1]));
     }
-    double bke = block_sum<kBlock>(ke, sh);
-    double bpe = block_sum<kBlock>(pe, sh);
+    const double bke = block_sum<kBlock>(ke, sh);
+    const double bpe = block_sum<kBlock>(pe, sh);
     if (threadIdx.x == 0) {
         partials[2 * blockIdx.x] = bke;
         partials[2 * blockIdx.x + 1] = bpe;
     }
-    if (last_block_done(&ds->ticket[1])) {
+    const unsigned int nblk = (unsigned int)(c.f_slots / kBlock);
+    if (last_block_done(&st.ticket[kStUpdate], nblk)) {
+        const int64_t b0 = c.f_slot / kBlock;
         double a = 0.0, b = 0.0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += kBlock) {
-            a += __ldcg(partials + 2 * i);
-            b += __ldcg(partials + 2 * i + 1);
+        for (int64_t i = threadIdx.x; i < (int64_t)nblk; i += kBlock) {
+            a += __ldcg(partials + 2 * (b0 + i));
+            b += __ldcg(partials + 2 * (b0 + i) + 1);
         }
         a = block_sum<kBlock>(a, sh);
         b = block_sum<kBlock>(b, sh);
         if (threadIdx.x == 0) {
-            ds->kinetic_energy = a;
-            ds->potential_energy = b;
-            ds->ticket[1] = 0;
-            dp->total_div_iter += ds->div_iter;
-            dp->total_incom_iter += ds->incom_iter;
-            dp->total_fbm_passes += ds->fbm_passes;
-            dp->max_dens_compression = fmax(dp->max_dens_compression, dp->compression);
+            st.kinetic_energy = a;
+            st.potential_energy = b;
+            st.ticket[kStUpdate] = 0;
+            ScenePersist &sp = k.sp[sc];
+            sp.total_div_iter += st.div_iter;
+            sp.total_incom_iter += st.incom_iter;
+            sp.total_fbm_passes += st.fbm_passes;
+            sp.max_dens_compression = fmax(sp.max_dens_compression, sp.compression);
+            sp.steps += 1;
         }
     }
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_unsort_bound(KConst k, tsph_set U, BoundBuf B,
+__global__ void __launch_bounds__(kBlock) k_update_bound(KConst k, tsph_set U, BoundBuf B,
                                                          const int *__restrict__ fstart) {
-    const int64_t pid = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (pid >= U.n) return;
-    const int s = B.inv[pid];
+    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (s >= B.cap) return;
+    const int sc = k.b_chunk_scene[s / kChunk];
+    const SceneConst &c = k.sc[sc];
+    if (s - c.b_slot >= c.b_n) return;
+    const SceneStep &st = k.ss[sc];
+    const int pid = B.perm[s];
     U.W[pid] = B.W[s];
     U.sph_density[pid] = B.rho[s];
     U.sph_compression[pid] = B.comp[s];
     U.alpha_2[pid] = B.a2[s];
     U.alpha[pid] = B.alpha[s];
-    const int code = U.neighb_cell_seq[pid];
-    if (code > 0 && code < k.node_num && s < B.start[k.node_num]) U.neighb_in_cell_seq[pid] = s + fstart[code + 1];
+    if (s - c.b_slot < st.b_in) {
+        const int code = U.neighb_cell_seq[pid];
+        U.neighb_in_cell_seq[pid] = (int)(s - st.b_shift) + fstart[c.cbase + code + 1];
+    }
 }
 
 // ----------------------------------------------------------------------------- neighbours
@@ -387,38 +440,43 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, const float4 *__restrict__ pos,
-                                                           const int *__restrict__ perm, int64_t n,
-                                                           FluidBuf F, BoundBuf B, int32_t *counts,
-                                                           uint64_t *hash) {
+__global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, FluidBuf F, BoundBuf B,
+                                                           int32_t *counts, uint64_t *hash) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= n) return;
-    const float4 pi = pos[s];
+    const int64_t cap = bound ? B.cap : F.cap;
+    if (s >= cap) return;
+    const int sc = bound ? k.b_chunk_scene[s / kChunk] : k.f_chunk_scene[s / kChunk];
+    const SceneConst &c = k.sc[sc];
+    if (s - (bound ? c.b_slot : c.f_slot) >= (bound ? c.b_n : c.f_n)) return;
+    const SceneStep &st = k.ss[sc];
+    Geo g;
+    g.load(c, k.R);
+    const float4 pi = bound ? B.pos[s] : F.pos[s];
     bool ok;
-    const long long code = cell_code<DIM>(pi, k, ok);
+    const long long code = cell_code<DIM>(pi, g, ok);
     int cf = 0, cb = 0;
     uint64_t hsum = 0;
     if (ok) {
-        visit_candidates<DIM>(F.start, k, code, [&](int j) {
+        visit_candidates<DIM>(F.start, g, code, st.f_shift, 0, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 > 0.f && sqrtf(r2) * k.inv_h < 1.f) {
+            if (r2 > 0.f && sqrtf(r2) * g.inv_h < 1.f) {
                 ++cf;
                 hsum += mix64((uint64_t)(uint32_t)F.perm[j]);
             }
         });
-        visit_candidates<DIM>(B.start, k, code, [&](int j) {
+        visit_candidates<DIM>(B.start, g, code, st.b_shift, 0, [&](int j) {
             const float4 pj = B.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 > 0.f && sqrtf(r2) * k.inv_h < 1.f) {
+            if (r2 > 0.f && sqrtf(r2) * g.inv_h < 1.f) {
                 ++cb;
                 hsum += mix64((1ull << 32) | (uint64_t)(uint32_t)B.perm[j]);
             }
         });
     }
-    const int pid = perm[s];
+    const int pid = bound ? B.perm[s] : F.perm[s];
     counts[2 * pid] = cf;
     counts[2 * pid + 1] = cb;
     hash[pid] = hsum;
@@ -426,7 +484,8 @@ __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, const float
 
 // ----------------------------------------------------------------------------- launchers
 void launch_step_begin(tsph_ctx &c, cudaStream_t st) {
-    cudaMemsetAsync(c.ds, 0, sizeof(DevStep), st);
+    cudaMemsetAsync(c.k.ss, 0, sizeof(SceneStep) * c.k.n_scenes, st);
+    cudaMemsetAsync(c.k.dg, 0, sizeof(DevGlobal), st);
 }
 
 void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st) {
@@ -434,22 +493,24 @@ void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st) {
     if (nb < 1) nb = 1;
     if (nb > 4 * 152) nb = 4 * 152;
     c.launches += 1;
-    if (c.k.dim == 3) k_cfl<3><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n, c.ds, c.dp);
-    else k_cfl<2><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n, c.ds, c.dp);
+    if (c.k.dim == 3) k_cfl<3><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n);
+    else k_cfl<2><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n);
 }
 
 void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st) {
-    const int64_t nn = c.k.node_num;
+    const int64_t nn = c.k.total_nodes;
     cudaMemsetAsync(c.F.count, 0, sizeof(int) * nn, st);
     cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, st);
-    c.launches += (f.n > 0) + (b.n > 0) + 3 + 1 + (f.n > 0) + (b.n > 0) + ((f.n > 0 || b.n > 0) ? 1 : 0);
+    const int S = c.k.n_scenes;
+    const int sb = (S + 127) / 128;
+    c.launches += (f.n > 0) + (b.n > 0) + 3 + 1 + (f.n > 0) + (b.n > 0) + 2 + 2;
     if (f.n > 0) {
-        if (c.k.dim == 3) k_encode<3><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, c.F.count, c.F.slot, &c.ds->f_tail, &c.ds->status);
-        else k_encode<2><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, c.F.count, c.F.slot, &c.ds->f_tail, &c.ds->status);
+        if (c.k.dim == 3) k_encode<3><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, 0, c.F.count, c.F.slot);
+        else k_encode<2><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, 0, c.F.count, c.F.slot);
     }
     if (b.n > 0) {
-        if (c.k.dim == 3) k_encode<3><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, c.B.count, c.B.slot, &c.ds->b_tail, &c.ds->status);
-        else k_encode<2><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, c.B.count, c.B.slot, &c.ds->b_tail, &c.ds->status);
+        if (c.k.dim == 3) k_encode<3><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, 1, c.B.count, c.B.slot);
+        else k_encode<2><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, 1, c.B.count, c.B.slot);
     }
     ScanArgs sa;
     sa.count[0] = c.F.count; sa.count[1] = c.B.count;
@@ -460,56 +521,40 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     k_scan_local<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa);
     k_scan_blocks<<<dim3(1, 2), kScanThreads, 0, st>>>(sa, nblk);
     k_scan_add<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk);
-    const int64_t nmax = f.n > b.n ? f.n : b.n;
-    if (nmax > 0) {
-        ScatterArgs sc;
-        sc.code[0] = f.neighb_cell_seq; sc.code[1] = b.neighb_cell_seq;
-        sc.slot[0] = c.F.slot; sc.slot[1] = c.B.slot;
-        sc.start[0] = c.F.start; sc.start[1] = c.B.start;
-        sc.perm[0] = c.F.perm; sc.perm[1] = c.B.perm;
-        sc.n[0] = f.n; sc.n[1] = b.n;
-        sc.node_num = nn;
-        k_scatter<<<dim3(blocks_for(nmax), 2), kBlock, 0, st>>>(sc);
-    }
-    CellSortArgs cs;
-    cs.start[0] = c.F.start; cs.start[1] = c.B.start;
-    cs.perm[0] = c.F.perm; cs.perm[1] = c.B.perm;
-    cs.n[0] = f.n; cs.n[1] = b.n;
-    cs.node_num = nn;
-    k_cell_sort<<<dim3(blocks_for(nn + 1), 2), kBlock, 0, st>>>(cs);
-    if (f.n > 0) {
-        if (c.k.dim == 3) k_gather_fluid<3><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, c.F);
-        else k_gather_fluid<2><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, c.F);
-    }
-    if (b.n > 0) {
-        if (c.k.dim == 3) k_gather_bound<3><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, c.B);
-        else k_gather_bound<2><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, c.B);
+    k_scene_shift<<<sb, 128, 0, st>>>(c.k, c.F.start, c.B.start);
+    if (f.n > 0) k_scatter<<<blocks_for(f.n), kBlock, 0, st>>>(c.k, 0, f.n, f.neighb_cell_seq, c.F.slot, c.F.start, c.F.perm);
+    if (b.n > 0) k_scatter<<<blocks_for(b.n), kBlock, 0, st>>>(c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm);
+    k_cell_sort<<<dim3(blocks_for(nn), 2), kBlock, 0, st>>>(c.k, c.F.start, c.F.perm, c.B.start, c.B.perm);
+    k_tail_sort<<<sb, 128, 0, st>>>(c.k, c.F.perm, c.B.perm);
+    if (c.k.dim == 3) {
+        k_gather_fluid<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F);
+        k_gather_bound<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, b, c.B);
+    } else {
+        k_gather_fluid<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F);
+        k_gather_bound<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, b, c.B);
     }
 }
 
 void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st) {
     const int fbm = c.p.fbm_enabled ? 1 : 0;
-    const int st_on = c.k.gamma != 0.f ? 1 : 0;
-    int nb = blocks_for(f.n);
-    if (nb < 1) nb = 1;
-    c.launches += 1 + (b.n > 0);
-    if (c.k.dim == 3) k_unsort_fluid<3><<<nb, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.ds, c.dp, c.S.partials, fbm, st_on);
-    else k_unsort_fluid<2><<<nb, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.ds, c.dp, c.S.partials, fbm, st_on);
-    if (b.n > 0) {
-        if (c.k.dim == 3) k_unsort_bound<3><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
-        else k_unsort_bound<2><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
+    const int st_on = c.st_on;
+    c.launches += 2;
+    if (c.k.dim == 3) {
+        k_update_fluid<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
+        k_update_bound<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
+    } else {
+        k_update_fluid<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
+        k_update_bound<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
     }
 }
 
-void launch_neighbor_stats(tsph_ctx &c, int64_t nf, int64_t nb, int32_t *fc, uint64_t *fh, int32_t *bc,
-                           uint64_t *bh, cudaStream_t st) {
-    if (nf > 0) {
-        if (c.k.dim == 3) k_neighbor_stats<3><<<blocks_for(nf), kBlock, 0, st>>>(c.k, c.F.pos, c.F.perm, nf, c.F, c.B, fc, fh);
-        else k_neighbor_stats<2><<<blocks_for(nf), kBlock, 0, st>>>(c.k, c.F.pos, c.F.perm, nf, c.F, c.B, fc, fh);
-    }
-    if (nb > 0) {
-        if (c.k.dim == 3) k_neighbor_stats<3><<<blocks_for(nb), kBlock, 0, st>>>(c.k, c.B.pos, c.B.perm, nb, c.F, c.B, bc, bh);
-        else k_neighbor_stats<2><<<blocks_for(nb), kBlock, 0, st>>>(c.k, c.B.pos, c.B.perm, nb, c.F, c.B, bc, bh);
+void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, uint64_t *bh, cudaStream_t st) {
+    if (c.k.dim == 3) {
+        k_neighbor_stats<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, 0, c.F, c.B, fc, fh);
+        k_neighbor_stats<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, 1, c.F, c.B, bc, bh);
+    } else {
+        k_neighbor_stats<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, 0, c.F, c.B, fc, fh);
+        k_neighbor_stats<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, 1, c.F, c.B, bc, bh);
     }
 }
 

@@ -83,7 +83,7 @@ __device__ __forceinline__ float4 load_pos(const float *pos, int64_t i) {
 }
 
 template <int DIM>
-__global__ void k_na_encode(KConst k, SetIn in, int *count, int *slot, int *tail) {
+__global__ void k_na_encode(Geo k, SetIn in, int *count, int *slot, int *tail) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= in.n) return;
     bool ok;
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(1024) k_na_scan(const int *count, int *start, 
 }
 
 template <int DIM>
-__global__ void k_na_scatter(KConst k, SetIn in, const int *slot, const int *start, int *perm) {
+__global__ void k_na_scatter(Geo k, SetIn in, const int *slot, const int *start, int *perm) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= in.n) return;
     const int sl = slot[i];
@@ -176,7 +176,7 @@ __global__ void k_na_sort(const int *start0, int *perm0, int64_t n0, const int *
 // boundary candidates (SPH_prepare_attr (f,f) then (f,b), sph.py:50-64), with
 // the same candidate order and arithmetic as the step's density sweep.
 template <int DIM>
-__global__ void k_na_density(KConst k, SetIn f, SetIn b, const int *fstart, const int *fperm, const int *bstart,
+__global__ void k_na_density(Geo k, SetIn f, SetIn b, const int *fstart, const int *fperm, const int *bstart,
                              const int *bperm, float *W, float *rho, float *comp) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= f.n) return;
@@ -185,7 +185,7 @@ __global__ void k_na_density(KConst k, SetIn f, SetIn b, const int *fstart, cons
     const long long code = cell_code<DIM>(pi, k, ok);
     float wsum = 0.f, rh = 0.f, cp = 0.f;
     if (ok) {
-        visit_candidates<DIM>(fstart, k, code, [&](int j) {
+        visit_candidates<DIM>(fstart, k, code, 0, 0, [&](int j) {
             const int pid = fperm[j];
             const float4 pj = load_pos<DIM>(f.pos, pid);
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -197,7 +197,7 @@ __global__ void k_na_density(KConst k, SetIn f, SetIn b, const int *fstart, cons
                 cp += w * f.rest_volume[pid];
             }
         });
-        visit_candidates<DIM>(bstart, k, code, [&](int j) {
+        visit_candidates<DIM>(bstart, k, code, 0, 0, [&](int j) {
             const int pid = bperm[j];
             const float4 pj = load_pos<DIM>(b.pos, pid);
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -273,7 +273,7 @@ extern "C" int tsph_fluid_density_noalloc(const tsph_params *p, const float *flu
     }
     const Grids g = carve(base);
 
-    KConst k = {};
+    Geo k = {};
     for (int d = 0; d < 3; ++d) k.lb[d] = d < p->dim ? p->lb[d] : 0.f;
     k.h = p->kernel_h;
     k.h2 = p->kernel_h2;
@@ -283,8 +283,8 @@ extern "C" int tsph_fluid_density_noalloc(const tsph_params *p, const float *flu
     k.node_num = p->node_num;
     k.nx = p->grid_size[0];
     k.nxny = (long long)p->grid_size[0] * (p->dim == 3 ? p->grid_size[1] : 1);
+    k.cbase = 0;
     k.R = p->neighb_range;
-    k.dim = p->dim;
 
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t nn = p->node_num;

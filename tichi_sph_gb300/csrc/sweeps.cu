@@ -1,19 +1,52 @@
 // Neighbour sweeps of one substep: density + alpha, the Jacobi pair of the two
 // pressure solves, and the advection forces (viscosity, surface tension).
 //
-// One thread per particle in cell-sorted order.  The density sweep scans the
-// (2r+1)^dim template rows of the fluid grid and, where the reference pairs with
-// the boundary set, of the boundary grid (visit_candidates), and records every
-// pair with 0 < r < h in the fluid particle's neighbour list.  The later sweeps
-// of the step walk that list (for_each_neighbor_tpp) -- about 30 entries instead
-// of about 220 candidates in 3D -- in the same order, so with one thread per
-// particle their sums are identical to a candidate scan.  Per-particle sums are FP32 (the reference's precision);
-// global sums are FP64 with a fixed summation order.
+// One thread (or TPP threads) per particle in cell-sorted order; a block never
+// straddles two scenes, so every block reads one scene's constants.  The
+// density sweep scans the (2r+1)^dim template rows of the fluid grid and, where
+// the reference pairs with the boundary set, of the boundary grid
+// (visit_candidates), and records every pair with 0 < r < h in the fluid
+// particle's neighbour list.  The later sweeps of the step walk that list
+// (for_each_neighbor_tpp) -- about 30 entries instead of about 220 candidates in
+// 3D -- in the same order.  Per-particle sums are FP32 (the reference's
+// precision); global sums are FP64 with a fixed summation order.
+//
+// Solver loops run per scene: a scene's loop state (iteration, condition,
+// v_adv buffer) lives in its SceneStep; blocks of a scene whose loop has ended
+// do nothing, the last block of a scene evaluates its loop test, and the last
+// block of the grid sets the CUDA-graph while condition to "any scene running".
 #include <cuda_runtime.h>
 
 #include "ctx.h"
 
 namespace tsph {
+
+// True for the warp of this block that finishes last (every warp must call it).
+__device__ __forceinline__ bool block_last_warp(unsigned int *arrived) {
+    unsigned int old = 0;
+    if ((threadIdx.x & 31) == 0) {
+        __threadfence_block();
+        old = atomicAdd(arrived, 1u);
+    }
+    old = __shfl_sync(0xffffffffu, old, 0);
+    const bool last = old == blockDim.x / 32 - 1;
+    if (last) __threadfence_block();
+    return last;
+}
+
+// The last warp of the grid: OR of the scenes' loop conditions into cond_any and
+// the graph condition.
+__device__ __forceinline__ void publish_any(const KConst &k, int SceneStep::*field, int32_t *any_out,
+                                            cudaGraphConditionalHandle h, int use_cond) {
+    const int lane = threadIdx.x & 31;
+    int any = 0;
+    for (int s = lane; s < k.n_scenes; s += 32) any |= (__ldcg(&(k.ss[s].*field)) != 0);
+    any = __any_sync(0xffffffffu, any);
+    if (lane == 0) {
+        *any_out = any;
+        if (use_cond) cudaGraphSetConditional(h, any ? 1u : 0u);
+    }
+}
 
 // ----------------------------------------------------------------------------- density
 // SPH_clean_value + SPH_prepare_attr (f,f)(f,b) + SPH_prepare_alpha_1 (f,f)(f,b)
@@ -26,22 +59,22 @@ namespace tsph {
 // recorded list is walked for the kernel arithmetic.  A particle whose pairs do
 // not fit the list redoes the scan with the arithmetic inline.
 template <int DIM>
-__device__ __forceinline__ void density_pair_fluid(const KConst &k, const FluidBuf &F, float4 pi, int j,
-                                                   float &wsum, float &rho, float &comp, float &a1x, float &a1y,
-                                                   float &a1z, float &a2) {
+__device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf &F, float4 pi, int j, float &wsum,
+                                                   float &rho, float &comp, float &a1x, float &a1y, float &a1z,
+                                                   float &a2) {
     const float4 pj = F.pos[j];
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < k.h2) {
+    if (r2 < g.h2) {
         const float2 mv = F.mv[j];
         const float r = sqrtf(r2);
-        const float q = r * k.inv_h;
-        const float w = kw(q) * k.sig;
+        const float q = r * g.inv_h;
+        const float w = kw(q) * g.sig;
         wsum += w;
         rho += w * mv.x;
         comp += w * mv.y;
         if (r2 > 0.f) {
-            const float wg = kwg(q) * k.sig_h;
+            const float wg = kwg(q) * g.sig_h;
             const float f = pj.w * wg / r;
             a1x += f * dx;
             a1y += f * dy;
@@ -52,22 +85,21 @@ __device__ __forceinline__ void density_pair_fluid(const KConst &k, const FluidB
 }
 
 template <int DIM>
-__device__ __forceinline__ void density_pair_bound(const KConst &k, const BoundBuf &B, float4 pi, int j,
-                                                   float &wsum, float &rho, float &comp, float &a1x, float &a1y,
-                                                   float &a1z) {
+__device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf &B, float4 pi, int j, float &wsum,
+                                                   float &rho, float &comp, float &a1x, float &a1y, float &a1z) {
     const float4 pj = B.pos[j];
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < k.h2) {
+    if (r2 < g.h2) {
         const float2 mv = B.mv[j];
         const float r = sqrtf(r2);
-        const float q = r * k.inv_h;
-        const float w = kw(q) * k.sig;
+        const float q = r * g.inv_h;
+        const float w = kw(q) * g.sig;
         wsum += w;
         rho += w * mv.x;
         comp += w * mv.y;
         if (r2 > 0.f) {
-            const float f = pj.w * kwg(q) * k.sig_h / r;
+            const float f = pj.w * kwg(q) * g.sig_h / r;
             a1x += f * dx;
             a1y += f * dy;
             a1z += f * dz;
@@ -76,26 +108,32 @@ __device__ __forceinline__ void density_pair_bound(const KConst &k, const BoundB
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf F, BoundBuf B, int64_t n) {
+__global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= n) return;
+    const int sc = k.f_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
+    const SceneConst &c = k.sc[sc];
+    if (s - c.f_slot >= c.f_n) return;
+    const SceneStep &st = k.ss[sc];
+    Geo g;
+    g.load(c, k.R);
+    const long long f_shift = st.f_shift, b_shift = st.b_shift;
     const float4 pi = F.pos[s];
     bool ok;
-    const long long code = cell_code<DIM>(pi, k, ok);
+    const long long code = cell_code<DIM>(pi, g, ok);
     float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f;
     float a1x = 0.f, a1y = 0.f, a1z = 0.f;
     int nfl = 0, nbo = 0;
     int *L = F.nbr;
     const int64_t stride = F.cap;
     const int cap = k.nbr_max;
-    const float w0 = kw(0.f) * k.sig;
+    const float w0 = kw(0.f) * g.sig;
     if (ok) {
         // phase 1: record the pairs
-        visit_candidates<DIM>(F.start, k, code, [&](int j) {
+        visit_candidates<DIM>(F.start, g, code, f_shift, 0, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < k.h2) {
+            if (r2 < g.h2) {
                 if (r2 > 0.f) {
                     if (nfl < cap) L[nbr_index(nfl, s, stride)] = j;
                     ++nfl;
@@ -107,11 +145,11 @@ __global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf 
                 }
             }
         });
-        visit_candidates<DIM>(B.start, k, code, [&](int j) {
+        visit_candidates<DIM>(B.start, g, code, b_shift, 0, [&](int j) {
             const float4 pj = B.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < k.h2) {
+            if (r2 < g.h2) {
                 if (r2 > 0.f) {
                     const int t = nfl + nbo;
                     if (t < cap) L[nbr_index(t, s, stride)] = j;
@@ -127,16 +165,16 @@ __global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf 
         if (nfl + nbo <= cap) {
             // phase 2: the arithmetic over the recorded pairs
             walk_blocks<1>(F.nbr, s, stride, 0, nfl, nfl + nbo,
-                [&](int j) { density_pair_fluid<DIM>(k, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2); },
-                [&](int j) { density_pair_bound<DIM>(k, B, pi, j, wsum, rho, comp, a1x, a1y, a1z); });
+                [&](int j) { density_pair_fluid<DIM>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2); },
+                [&](int j) { density_pair_bound<DIM>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z); });
         } else {
             // list overflow: one scan with the arithmetic inline
             wsum = rho = comp = a2 = a1x = a1y = a1z = 0.f;
-            visit_candidates<DIM>(F.start, k, code, [&](int j) {
-                density_pair_fluid<DIM>(k, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
+            visit_candidates<DIM>(F.start, g, code, f_shift, 0, [&](int j) {
+                density_pair_fluid<DIM>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
             });
-            visit_candidates<DIM>(B.start, k, code, [&](int j) {
-                density_pair_bound<DIM>(k, B, pi, j, wsum, rho, comp, a1x, a1y, a1z);
+            visit_candidates<DIM>(B.start, g, code, b_shift, 0, [&](int j) {
+                density_pair_bound<DIM>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z);
             });
         }
     }
@@ -155,39 +193,44 @@ __global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf 
 // The boundary's own sums: SPH_prepare_attr (b,b)(b,f), SPH_prepare_alpha_2 (b,f),
 // SPH_prepare_alpha (sph.py:50-105 as called by main.py:190-197).
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, BoundBuf B, int64_t n) {
+__global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= n) return;
+    const int sc = k.b_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
+    const SceneConst &c = k.sc[sc];
+    if (s - c.b_slot >= c.b_n) return;
+    const SceneStep &st = k.ss[sc];
+    Geo g;
+    g.load(c, k.R);
     const float4 pi = B.pos[s];
     bool ok;
-    const long long code = cell_code<DIM>(pi, k, ok);
+    const long long code = cell_code<DIM>(pi, g, ok);
     float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f;
     if (ok) {
-        visit_candidates<DIM>(B.start, k, code, [&](int j) {
+        visit_candidates<DIM>(B.start, g, code, st.b_shift, 0, [&](int j) {
             const float4 pj = B.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < k.h2) {
+            if (r2 < g.h2) {
                 const float2 mv = B.mv[j];
-                const float w = kw(sqrtf(r2) * k.inv_h) * k.sig;
+                const float w = kw(sqrtf(r2) * g.inv_h) * g.sig;
                 wsum += w;
                 rho += w * mv.x;
                 comp += w * mv.y;
             }
         });
-        visit_candidates<DIM>(F.start, k, code, [&](int j) {
+        visit_candidates<DIM>(F.start, g, code, st.f_shift, 0, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < k.h2) {
+            if (r2 < g.h2) {
                 const float2 mv = F.mv[j];
-                const float q = sqrtf(r2) * k.inv_h;
-                const float w = kw(q) * k.sig;
+                const float q = sqrtf(r2) * g.inv_h;
+                const float w = kw(q) * g.sig;
                 wsum += w;
                 rho += w * mv.x;
                 comp += w * mv.y;
                 if (r2 > 0.f) {
-                    const float wg = kwg(q) * k.sig_h;
+                    const float wg = kwg(q) * g.sig_h;
                     a2 += wg * wg * pj.w * pj.w / mv.x;
                 }
             }
@@ -205,50 +248,84 @@ __global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, 
 }
 
 // ----------------------------------------------------------------------------- solver
-// Sets the loop condition before a solve: main.py:201 / main.py:222 test
-// `iter < iter_min or compression > tol` with the compression left by the
-// previous solve.  `flip` makes the v_adv written by the advection sweep current.
-__global__ void k_solve_begin(KConst k, DevStep *ds, const DevPersist *dp, int kind, int flip,
-                              cudaGraphConditionalHandle h, int use_cond) {
-    const double tol = kind == kSolveDiv ? (double)k.div_tol : (double)k.comp_tol;
-    const int cond = (0 < k.iter_min) || (dp->compression > tol);
-    ds->iter = 0;
-    ds->cond = cond;
-    if (kind == kSolveDiv) ds->div_iter = 0;
-    else ds->incom_iter = 0;
-    if (flip) ds->cur = 1 - ds->cur;
-    if (use_cond) cudaGraphSetConditional(h, cond ? 1u : 0u);
+// Sets every scene's loop condition before a solve: main.py:201 / main.py:222
+// test `iter < iter_min or compression > tol` with the compression left by the
+// previous solve.  A scene without fluid runs min(iter_min, iter_max + 1) empty
+// iterations in the reference and its compression becomes 0/0 = NaN
+// (sph.py:226); that is settled here without device work.  `flip` makes the
+// v_adv written by the advection sweep current.
+__global__ void k_solve_begin(KConst k, int kind, int flip, cudaGraphConditionalHandle h, int use_cond) {
+    __shared__ int any_sh;
+    if (threadIdx.x == 0) any_sh = 0;
+    __syncthreads();
+    int any = 0;
+    for (int s = threadIdx.x; s < k.n_scenes; s += blockDim.x) {
+        const SceneConst &c = k.sc[s];
+        SceneStep &st = k.ss[s];
+        ScenePersist &sp = k.sp[s];
+        const double tol = kind == kSolveDiv ? (double)c.div_tol : (double)c.comp_tol;
+        int cond, it = 0;
+        if (c.f_n > 0) {
+            cond = (0 < c.iter_min) || (sp.compression > tol);
+        } else {
+            cond = 0;
+            while (it < c.iter_min) {
+                ++it;
+                if (it > c.iter_max) break;
+            }
+            if (it > 0) sp.compression = __longlong_as_double(0x7ff8000000000000ll);
+        }
+        st.iter = it;
+        st.cond = cond;
+        if (kind == kSolveDiv) st.div_iter = it;
+        else st.incom_iter = it;
+        if (flip) st.cur = 1 - st.cur;
+        any |= cond;
+    }
+    if (any) atomicOr(&any_sh, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        k.dg->cond_any = any_sh;
+        if (use_cond) cudaGraphSetConditional(h, any_sh ? 1u : 0u);
+    }
 }
 
 // Sweep A: IPPE_adv_psi_init + IPPE_adv_psi (f,f)(f,b) + IPPE_psi_adv_non_negative
 // (sph.py:196-226), TPP threads per particle.  Writes psi_adv and kappa =
-// psi_adv / alpha; the sum of psi_adv / psi0 goes to per-block partials and,
-// through the last warp of the grid, to ds->psi_sum (block order, deterministic).
+// psi_adv / alpha; the scene's sum of psi_adv / psi0 goes to per-block partials
+// and, through the scene's last block, to its psi_sum (block order:
+// deterministic).
 template <int DIM, int TPP>
-__global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B, int64_t n, DevStep *ds,
-                                                const DevPersist *dp, double *partials) {
+__global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B, double *partials) {
     __shared__ double sh[kBlock / 32];
     __shared__ unsigned int arrived;
+    const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
+    const int sc = k.f_chunk_scene[first / kChunk];
+    SceneStep &st = k.ss[sc];
+    if (!st.cond) return;  // this scene's loop has ended (uniform over the block)
     if (threadIdx.x == 0) arrived = 0;
     __syncthreads();
+    const SceneConst &c = k.sc[sc];
     const Lanes<TPP> ln;
     const int64_t s = ln.s;
-    const bool act = s < n;
-    const float4 *vin = F.vadv + ds->cur * F.cap;
+    const bool act = s - c.f_slot < c.f_n;
+    Geo g;
+    g.load(c, k.R);
+    const float4 *vin = F.vadv + st.cur * F.cap;
     float acc = 0.f;
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), vi = pi;
     if (act) {
         pi = F.pos[s];
         vi = vin[s];
-        for_each_neighbor_tpp<DIM, true, TPP>(k, F, B, s, ln.q, pi,
+        for_each_neighbor_tpp<DIM, true, TPP>(g, F, B, st.f_shift, st.b_shift, s, ln.q, pi,
             [&](int j) {
                 const float4 pj = F.pos[j];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < k.h2 && r2 > 0.f) {
+                if (r2 < g.h2 && r2 > 0.f) {
                     const float4 vj = vin[j];
                     const float r = sqrtf(r2);
-                    const float f = kwg(r * k.inv_h) * k.sig_h / r * pj.w;
+                    const float f = kwg(r * g.inv_h) * g.sig_h / r * pj.w;
                     acc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
                 }
             },
@@ -256,10 +333,10 @@ __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B
                 const float4 pj = B.pos[j];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < k.h2 && r2 > 0.f) {
+                if (r2 < g.h2 && r2 > 0.f) {
                     const float4 vj = B.vadv[j];
                     const float r = sqrtf(r2);
-                    const float f = kwg(r * k.inv_h) * k.sig_h / r * pj.w;
+                    const float f = kwg(r * g.inv_h) * g.sig_h / r * pj.w;
                     acc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
                 }
             });
@@ -268,7 +345,7 @@ __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B
     double contrib = 0.0;
     if (act && ln.q == 0) {
         const float4 mp = F.mpsi[s];
-        float psi = (mp.y - mp.z) + acc * dp->dt;
+        float psi = (mp.y - mp.z) + acc * k.sp[sc].dt;
         if (psi < 0.f) psi = 0.f;
         F.psiadv[s] = psi;
         F.kappa[s] = psi / mp.w;
@@ -277,113 +354,137 @@ __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B
     double bsum;
     if (block_sum_last_warp<kBlock>(contrib, sh, &arrived, bsum)) {
         if ((threadIdx.x & 31) == 0) partials[blockIdx.x] = bsum;
-        if (last_warp_done(&ds->ticket[4], gridDim.x)) {
+        const int64_t b0 = c.f_slot * TPP / kBlock;
+        const unsigned int nblk = (unsigned int)(c.f_slots * TPP / kBlock);
+        if (last_warp_done(&st.ticket[kStPsi], nblk)) {
             const int lane = threadIdx.x & 31;
             double v = 0.0;
-            for (int i = lane; i < (int)gridDim.x; i += 32) v += __ldcg(partials + i);
+            for (int64_t i = lane; i < (int64_t)nblk; i += 32) v += __ldcg(partials + b0 + i);
             v = warp_sum(v);
             if (lane == 0) {
-                ds->psi_sum = v;
-                ds->ticket[4] = 0;
+                st.psi_sum = v;
+                st.ticket[kStPsi] = 0;
             }
         }
     }
 }
 
-// Sweep B: IPPE_update_vel_adv (f,f)(f,b), sph.py:229-244, into the other v_adv
-// buffer, TPP threads per particle.  The last warp of the grid evaluates the loop
-// test of main.py:201-213 / 222-234 from sweep A's sum and sets the graph's
-// while-node condition.
+// Sweep B: IPPE_update_vel_adv (f,f)(f,b), sph.py:229-244, into the scene's other
+// v_adv buffer, TPP threads per particle.  The scene's last block evaluates the
+// loop test of main.py:201-213 / 222-234 from sweep A's sum; the grid's last
+// block sets the graph's while-node condition.
 template <int DIM, int TPP>
-__global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B, int64_t n, DevStep *ds,
-                                                DevPersist *dp, int kind, cudaGraphConditionalHandle h,
-                                                int use_cond) {
-    const Lanes<TPP> ln;
-    const int64_t s = ln.s;
-    const bool act = s < n;
-    const int cur = ds->cur;
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    if (act) {
-        const float4 pi = F.pos[s];
-        const float ki = F.kappa[s];
-        const float Xi = pi.w;
-        for_each_neighbor_tpp<DIM, true, TPP>(k, F, B, s, ln.q, pi,
-            [&](int j) {
-                const float4 pj = F.pos[j];
-                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < k.h2 && r2 > 0.f) {
-                    const float kj = F.kappa[j];
-                    const float r = sqrtf(r2);
-                    const float f = (ki * pj.w + kj * Xi) * (kwg(r * k.inv_h) * k.sig_h / r);
-                    ax += f * dx;
-                    ay += f * dy;
-                    az += f * dz;
-                }
-            },
-            [&](int j) {
-                const float4 pj = B.pos[j];
-                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < k.h2 && r2 > 0.f) {
-                    const float kj = B.kappa[j];
-                    const float r = sqrtf(r2);
-                    const float f = (ki * pj.w + kj * Xi) * (kwg(r * k.inv_h) * k.sig_h / r);
-                    ax += f * dx;
-                    ay += f * dy;
-                    az += f * dz;
-                }
-            });
-    }
-    ax = ln.sum(ax);
-    ay = ln.sum(ay);
-    az = ln.sum(az);
-    if (act && ln.q == 0) {
-        const float4 *vin = F.vadv + cur * F.cap;
-        float4 *vout = F.vadv + (1 - cur) * F.cap;
-        const float sc = -(1.f / dp->dt) / F.mpsi[s].x;
-        const float4 vi = vin[s];
-        vout[s] = make_float4(vi.x + sc * ax, vi.y + sc * ay, vi.z + sc * az, 0.f);
-    }
-    const unsigned int nwarps = (unsigned int)(gridDim.x * (kBlock / 32));
-    if (last_warp_done(&ds->ticket[2], nwarps)) {
-        if ((threadIdx.x & 31) == 0) {
-            const double comp = __ldcg(&ds->psi_sum) / (double)n;
-            dp->compression = comp;
-            const int it = ds->iter + 1;
-            ds->iter = it;
-            if (kind == kSolveDiv) ds->div_iter = it;
-            else ds->incom_iter = it;
-            const double tol = kind == kSolveDiv ? (double)k.div_tol : (double)k.comp_tol;
-            const int capped = it > k.iter_max;
-            const int cond = !capped && (it < k.iter_min || comp > tol);
-            if (capped) ds->status |= (kind == kSolveDiv ? TSPH_ST_DIV_ITER_CAP : TSPH_ST_DENS_ITER_CAP);
-            ds->cond = cond;
-            ds->cur = 1 - cur;
-            ds->ticket[2] = 0;
-            if (use_cond) cudaGraphSetConditional(h, cond ? 1u : 0u);
+__global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B, int kind,
+                                                cudaGraphConditionalHandle h, int use_cond) {
+    __shared__ unsigned int arrived;
+    if (threadIdx.x == 0) arrived = 0;
+    __syncthreads();
+    const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
+    const int sc = k.f_chunk_scene[first / kChunk];
+    SceneStep &st = k.ss[sc];
+    const SceneConst &c = k.sc[sc];
+    const bool running = st.cond != 0;
+    if (running) {
+        const Lanes<TPP> ln;
+        const int64_t s = ln.s;
+        const bool act = s - c.f_slot < c.f_n;
+        Geo g;
+        g.load(c, k.R);
+        const int cur = st.cur;
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        if (act) {
+            const float4 pi = F.pos[s];
+            const float ki = F.kappa[s];
+            const float Xi = pi.w;
+            for_each_neighbor_tpp<DIM, true, TPP>(g, F, B, st.f_shift, st.b_shift, s, ln.q, pi,
+                [&](int j) {
+                    const float4 pj = F.pos[j];
+                    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 < g.h2 && r2 > 0.f) {
+                        const float kj = F.kappa[j];
+                        const float r = sqrtf(r2);
+                        const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h / r);
+                        ax += f * dx;
+                        ay += f * dy;
+                        az += f * dz;
+                    }
+                },
+                [&](int j) {
+                    const float4 pj = B.pos[j];
+                    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 < g.h2 && r2 > 0.f) {
+                        const float kj = B.kappa[j];
+                        const float r = sqrtf(r2);
+                        const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h / r);
+                        ax += f * dx;
+                        ay += f * dy;
+                        az += f * dz;
+                    }
+                });
         }
+        ax = ln.sum(ax);
+        ay = ln.sum(ay);
+        az = ln.sum(az);
+        if (act && ln.q == 0) {
+            const float4 *vin = F.vadv + cur * F.cap;
+            float4 *vout = F.vadv + (1 - cur) * F.cap;
+            const float sc_ = -(1.f / k.sp[sc].dt) / F.mpsi[s].x;
+            const float4 vi = vin[s];
+            vout[s] = make_float4(vi.x + sc_ * ax, vi.y + sc_ * ay, vi.z + sc_ * az, 0.f);
+        }
+    }
+    if (!block_last_warp(&arrived)) return;
+    if (running) {
+        const unsigned int nblk = (unsigned int)(c.f_slots * TPP / kBlock);
+        if (last_warp_done(&st.ticket[kStVel], nblk) && (threadIdx.x & 31) == 0) {
+            ScenePersist &sp = k.sp[sc];
+            const double comp = st.psi_sum / (double)c.f_n;
+            sp.compression = comp;
+            const int it = st.iter + 1;
+            st.iter = it;
+            if (kind == kSolveDiv) st.div_iter = it;
+            else st.incom_iter = it;
+            const double tol = kind == kSolveDiv ? (double)c.div_tol : (double)c.comp_tol;
+            const int capped = it > c.iter_max;
+            const int cond = !capped && (it < c.iter_min || comp > tol);
+            if (capped) st.status |= (kind == kSolveDiv ? TSPH_ST_DIV_ITER_CAP : TSPH_ST_DENS_ITER_CAP);
+            st.cond = cond;
+            st.cur = 1 - st.cur;
+            st.ticket[kStVel] = 0;
+        }
+    }
+    if (last_warp_done(&k.dg->ticket[kGtVel], gridDim.x)) {
+        publish_any(k, &SceneStep::cond, &k.dg->cond_any, h, use_cond);
+        if ((threadIdx.x & 31) == 0) k.dg->ticket[kGtVel] = 0;
     }
 }
 
 // ----------------------------------------------------------------------------- advection
 // First pass of SPH_advection_surface_tension_acc, sph.py:134-150: surface normals.
 template <int DIM, int TPP>
-__global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBuf B, int64_t n) {
+__global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBuf B) {
+    const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
+    const int sc = k.f_chunk_scene[first / kChunk];
+    const SceneConst &c = k.sc[sc];
+    const SceneStep &st = k.ss[sc];
     const Lanes<TPP> ln;
     const int64_t s = ln.s;
-    const bool act = s < n;
+    const bool act = s - c.f_slot < c.f_n;
+    Geo g;
+    g.load(c, k.R);
     float nx = 0.f, ny = 0.f, nz = 0.f;
     if (act) {
         const float4 pi = F.pos[s];
-        for_each_neighbor_tpp<DIM, false, TPP>(k, F, B, s, ln.q, pi,
+        for_each_neighbor_tpp<DIM, false, TPP>(g, F, B, st.f_shift, st.b_shift, s, ln.q, pi,
             [&](int j) {
                 const float4 pj = F.pos[j];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < k.h2 && r2 > 0.f) {
+                if (r2 < g.h2 && r2 > 0.f) {
                     const float r = sqrtf(r2);
-                    const float f = -pj.w / F.mpsi[j].y * (kwg(r * k.inv_h) * k.sig_h) / r;
+                    const float f = -pj.w / F.mpsi[j].y * (kwg(r * g.inv_h) * g.sig_h) / r;
                     nx += f * dx;
                     ny += f * dy;
                     nz += f * dz;
@@ -394,7 +495,7 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
     nx = ln.sum(nx);
     ny = ln.sum(ny);
     nz = ln.sum(nz);
-    if (act && ln.q == 0) F.normal[s] = make_float4(nx * k.h, ny * k.h, nz * k.h, 0.f);
+    if (act && ln.q == 0) F.normal[s] = make_float4(nx * g.h, ny * g.h, nz * g.h, 0.f);
 }
 
 // SPH_vel_adv_2_vel + SPH_advection_gravity_acc + SPH_advection_viscosity_acc
@@ -404,12 +505,17 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
 // template cells, not only those within h: with surface tension on this sweep
 // scans the cells; without it, it walks the neighbour list.
 template <int DIM, bool ST, int TPP>
-__global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBuf B, int64_t n,
-                                                   const DevStep *ds, const DevPersist *dp) {
+__global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBuf B) {
+    const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
+    const int sc = k.f_chunk_scene[first / kChunk];
+    const SceneConst &c = k.sc[sc];
+    const SceneStep &st = k.ss[sc];
     const Lanes<TPP> ln;
     const int64_t s = ln.s;
-    const bool act = s < n;
-    const int cur = ds->cur;
+    const bool act = s - c.f_slot < c.f_n;
+    Geo g;
+    g.load(c, k.R);
+    const int cur = st.cur;
     const float4 *vin = F.vadv + cur * F.cap;
     float vx = 0.f, vy = 0.f, vz = 0.f;   // viscosity sum
     float sx = 0.f, sy = 0.f, sz = 0.f;   // surface tension sum
@@ -422,17 +528,18 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
         const float4 ni = ST ? F.normal[s] : make_float4(0.f, 0.f, 0.f, 0.f);
         const bool st_i = ST && vfi0 > 0.99f;
         const float lap = 2.f * (2.f + DIM);
-        const float eps = 0.01f * k.h2;
+        const float eps = 0.01f * g.h2;
+        const float gamma = c.gamma, c_coh = c.c_coh;
         auto pair = [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (!(r2 > 0.f)) return;
-            if (r2 < k.h2) {
+            if (r2 < g.h2) {
                 const float4 vj = vin[j];
                 const float psij = F.mpsi[j].y;
                 const float r = sqrtf(r2);
-                const float wg = kwg(r * k.inv_h) * k.sig_h;
+                const float wg = kwg(r * g.inv_h) * g.sig_h;
                 const float adx = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
                 const float f = lap * (pj.w / psij) * wg / r * adx / (eps + r2);
                 vx += f * dx;
@@ -444,20 +551,21 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                     const float4 mpj = F.mpsi[j];
                     const float4 nj = F.normal[j];
                     const float r = sqrtf(r2);
-                    const float coh = -k.gamma * mpj.x * (kcoh(r * k.inv_h) * k.c_coh) / r;
+                    const float coh = -gamma * mpj.x * (kcoh(r * g.inv_h) * c_coh) / r;
                     const float fac = 2.f * mpi.z / (mpi.y + mpj.y);
-                    sx += fac * (coh * dx + k.gamma * (ni.x - nj.x));
-                    sy += fac * (coh * dy + k.gamma * (ni.y - nj.y));
-                    sz += fac * (coh * dz + k.gamma * (ni.z - nj.z));
+                    sx += fac * (coh * dx + gamma * (ni.x - nj.x));
+                    sy += fac * (coh * dy + gamma * (ni.y - nj.y));
+                    sz += fac * (coh * dz + gamma * (ni.z - nj.z));
                 }
             }
         };
         if (ST) {
             bool ok;
-            const long long code = cell_code<DIM>(pi, k, ok);
-            if (ok) visit_candidates_strided<DIM, TPP>(F.start, k, code, ln.q, pair);
+            const long long code = cell_code<DIM>(pi, g, ok);
+            if (ok) visit_candidates<DIM, TPP>(F.start, g, code, st.f_shift, ln.q, pair);
         } else {
-            for_each_neighbor_tpp<DIM, false, TPP>(k, F, B, s, ln.q, pi, pair, [&](int) {});
+            for_each_neighbor_tpp<DIM, false, TPP>(g, F, B, st.f_shift, st.b_shift, s, ln.q, pi, pair,
+                                                   [&](int) {});
         }
     }
     vx = ln.sum(vx);
@@ -470,11 +578,11 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
     }
     if (act && ln.q == 0) {
         float4 *vout = F.vadv + (1 - cur) * F.cap;
-        const float dt = dp->dt;
-        const float mu = k.mu / F.rho0[s];
-        const float ax = k.g[0] + vx * mu + sx;
-        const float ay = k.g[1] + vy * mu + sy;
-        const float az = (DIM == 3 ? k.g[2] : 0.f) + vz * mu + sz;
+        const float dt = k.sp[sc].dt;
+        const float mu = c.mu / F.rho0[s];
+        const float ax = c.g[0] + vx * mu + sx;
+        const float ay = c.g[1] + vy * mu + sy;
+        const float az = (DIM == 3 ? c.g[2] : 0.f) + vz * mu + sz;
         F.acc[s] = make_float4(ax, ay, az, 0.f);
         F.vel[s] = vi;
         vout[s] = make_float4(vi.x + ax * dt, vi.y + ay * dt, vi.z + az * dt, 0.f);
@@ -482,78 +590,75 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
 }
 
 // ----------------------------------------------------------------------------- launchers
-void launch_density(tsph_ctx &c, int64_t nf, int64_t nb, cudaStream_t st) {
-    c.launches += (nf > 0) + (nb > 0);
-    if (nf > 0) {
-        if (c.k.dim == 3) k_density_fluid<3><<<blocks_for(nf), kBlock, 0, st>>>(c.k, c.F, c.B, nf);
-        else k_density_fluid<2><<<blocks_for(nf), kBlock, 0, st>>>(c.k, c.F, c.B, nf);
-    }
-    if (nb > 0) {
-        if (c.k.dim == 3) k_density_bound<3><<<blocks_for(nb), kBlock, 0, st>>>(c.k, c.F, c.B, nb);
-        else k_density_bound<2><<<blocks_for(nb), kBlock, 0, st>>>(c.k, c.F, c.B, nb);
+void launch_density(tsph_ctx &c, cudaStream_t st) {
+    c.launches += 2;
+    if (c.k.dim == 3) {
+        k_density_fluid<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+        k_density_bound<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+    } else {
+        k_density_fluid<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+        k_density_bound<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
     }
 }
 
 void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
     c.launches += 1;
-    k_solve_begin<<<1, 1, 0, st>>>(c.k, c.ds, c.dp, kind, kind == kSolveDens ? 1 : 0, h, use_cond);
+    k_solve_begin<<<1, 256, 0, st>>>(c.k, kind, kind == kSolveDens ? 1 : 0, h, use_cond);
 }
 
 // Threads per particle of the list sweeps (1, 2, 4 or 8); see Lanes.
 #define TSPH_TPP_DISPATCH(TPP_VAL, ...)                                   \
     switch (TPP_VAL) {                                                     \
-        case 1: { constexpr int TPP = 1; __VA_ARGS__; } break;             \
         case 2: { constexpr int TPP = 2; __VA_ARGS__; } break;             \
+        case 4: { constexpr int TPP = 4; __VA_ARGS__; } break;             \
         case 8: { constexpr int TPP = 8; __VA_ARGS__; } break;             \
-        default: { constexpr int TPP = 4; __VA_ARGS__; } break;            \
+        default: { constexpr int TPP = 1; __VA_ARGS__; } break;            \
     }
 
-static int tpp_blocks(int64_t n, int tpp) { return blocks_for(n * tpp); }
+static int tpp_blocks(int64_t slots, int tpp) { return blocks_for(slots * tpp); }
 
-void launch_psi(tsph_ctx &c, int64_t nf, cudaStream_t st) {
+void launch_psi(tsph_ctx &c, cudaStream_t st) {
     c.launches += 1;
     const int tpp = c.tpp;
-    const int nb = tpp_blocks(nf, tpp);
+    const int nb = tpp_blocks(c.F.cap, tpp);
     TSPH_TPP_DISPATCH(tpp,
-        if (c.k.dim == 3) k_psi<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf, c.ds, c.dp, c.S.partials);
-        else k_psi<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf, c.ds, c.dp, c.S.partials));
+        if (c.k.dim == 3) k_psi<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
+        else k_psi<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials));
 }
 
-void launch_vel(tsph_ctx &c, int64_t nf, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
     c.launches += 1;
     const int tpp = c.tpp;
-    const int nb = tpp_blocks(nf, tpp);
+    const int nb = tpp_blocks(c.F.cap, tpp);
     TSPH_TPP_DISPATCH(tpp,
-        if (c.k.dim == 3) k_vel<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf, c.ds, c.dp, kind, h, use_cond);
-        else k_vel<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf, c.ds, c.dp, kind, h, use_cond));
+        if (c.k.dim == 3) k_vel<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond);
+        else k_vel<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond));
 }
 
-void launch_solve_iter(tsph_ctx &c, int64_t nf, int kind, cudaGraphConditionalHandle h, int use_cond,
-                       cudaStream_t st) {
-    launch_psi(c, nf, st);
-    launch_vel(c, nf, kind, h, use_cond, st);
+void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+    launch_psi(c, st);
+    launch_vel(c, kind, h, use_cond, st);
 }
 
-void launch_advect(tsph_ctx &c, int64_t nf, cudaStream_t st) {
-    if (nf <= 0) return;
+void launch_advect(tsph_ctx &c, cudaStream_t st) {
     const int tpp = c.tpp;
-    const int nb = tpp_blocks(nf, tpp);
-    const bool st_on = c.k.gamma != 0.f;
+    const int nb = tpp_blocks(c.F.cap, tpp);
+    const bool st_on = c.st_on != 0;
     c.launches += st_on ? 2 : 1;
     TSPH_TPP_DISPATCH(tpp,
         if (c.k.dim == 3) {
             if (st_on) {
-                k_normal<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf);
-                k_advect<3, true, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf, c.ds, c.dp);
+                k_normal<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<3, true, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
             } else {
-                k_advect<3, false, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf, c.ds, c.dp);
+                k_advect<3, false, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
             }
         } else {
             if (st_on) {
-                k_normal<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf);
-                k_advect<2, true, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf, c.ds, c.dp);
+                k_normal<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<2, true, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
             } else {
-                k_advect<2, false, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, nf, c.ds, c.dp);
+                k_advect<2, false, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
             }
         });
 }

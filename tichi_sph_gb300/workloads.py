@@ -66,3 +66,71 @@ def dambreak_3d(n_side=100, spacing=0.01):
             _obj("box", [-0.035, -0.035, -0.035], [3.035, 1.535, 1.035], [1], [0, 0, 0], layers=3)]},
     }
     return cfg, scen
+
+
+def twophase_3d(n_side=100, spacing=0.01, seed=3):
+    """3D two-phase VFSPH: two 1 m cubes side by side (rest densities 1000 and 500)
+    in the 3 x 1.5 x 1 m tank, surface tension 0.07, the volume-fraction update on.
+    The reference has one global viscosity (sph.py:129): 0.01 stands for the
+    0.01 / 0.05 pair.  Returns (config, scenario, volume-fraction noise function)."""
+    import numpy as np
+    L = n_side * spacing
+    cfg = _config(solver="VFSPH", cs=50, gamma=0.07, fbm_c=50.0, fbm_d=0.0)
+    scen = {
+        "sim_env": {"global_part_size": spacing, "global_dynamic_viscosity": 0.01, "sim_dim": 3,
+                    "sim_space_lb": [-0.15, -0.15, -0.15], "sim_space_rt": [3.2, 2.0, 1.2],
+                    "gravity": [0, -9.81, 0], "phase_num": 2, "phase_rest_density": [1000, 500],
+                    "phase_color_hex": ["0x6F7DBC", "0xFA8012"]},
+        "fluid": {"max_part_num": 2 * n_side ** 3, "objs": [
+            _obj("cube", [0.0, 0.0, 0.0], [L, L, L], [1, 0], [0, 0, 0]),
+            _obj("cube", [L + spacing, 0.0, 0.0], [2 * L + spacing, L, L], [0, 1], [0, 0, 0])]},
+        "bound": {"max_part_num": 566742, "objs": [
+            _obj("box", [-0.035, -0.035, -0.035], [3.035, 1.535, 1.035], [1, 0], [0, 0, 0], layers=3)]},
+    }
+
+    def noise(vf):
+        """Seeded U(-0.05, 0.05) on phase 0, clipped to [0, 1]; phase 1 = 1 - phase 0."""
+        rng = np.random.default_rng(seed)
+        v0 = np.clip(vf[:, 0] + rng.uniform(-0.05, 0.05, len(vf)), 0.0, 1.0).astype(np.float32)
+        out = np.stack([v0, (1.0 - v0).astype(np.float32)], axis=1)
+        return out
+    return cfg, scen, noise
+
+
+def batched_dambreaks(n_scenes=256, seed=4, spacing=0.01, n_min=2000, n_max=200000):
+    """Independent 3D dam breaks of uneven size: fluid counts log-uniform in
+    [n_min, n_max], block aspect ratios x/y and z/y uniform in [0.5, 2], rest
+    density uniform in [800, 1200], each block in the x-min corner of its own tank
+    (2.5 x 1.5 x 1 block lengths, 3 boundary layers).  Returns a list of
+    (config, scenario) pairs."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_scenes):
+        n = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        ax, az = rng.uniform(0.5, 2.0), rng.uniform(0.5, 2.0)
+        ny = max(2, int(round((n / (ax * az)) ** (1.0 / 3.0))))
+        nx, nz = max(2, int(round(ax * ny))), max(2, int(round(az * ny)))
+        Lx, Ly, Lz = nx * spacing, ny * spacing, nz * spacing
+        rho = float(rng.uniform(800.0, 1200.0))
+        t = 3.5 * spacing
+        box_lo = [-t, -t, -t]
+        box_hi = [2.5 * Lx + t, 1.5 * Ly + t, Lz + t]
+        # boundary count with the emitter's arithmetic (sph_obj.py:102-107, 140-151)
+        sp32 = float(np.float32(spacing))
+        shape = ((np.array(box_hi, np.float32) - np.array(box_lo, np.float32) + 1e-7) / sp32).astype(np.int32)
+        n_box = int(np.prod(shape.astype(np.int64)) - np.prod(np.maximum(shape.astype(np.int64) - 6, 0)))
+        cfg = _config(cs=50)
+        scen = {
+            "sim_env": {"global_part_size": spacing, "global_dynamic_viscosity": 0.01, "sim_dim": 3,
+                        "sim_space_lb": [b - 0.1 for b in box_lo],
+                        "sim_space_rt": [box_hi[0] + 0.1, box_hi[1] + 0.1 + 0.5 * Ly, box_hi[2] + 0.1],
+                        "gravity": [0, -9.81, 0], "phase_num": 1, "phase_rest_density": [rho],
+                        "phase_color_hex": ["0x6F7DBC"]},
+            "fluid": {"max_part_num": nx * ny * nz, "objs": [
+                _obj("cube", [0.0, 0.0, 0.0], [Lx, Ly, Lz], [1], [0, 0, 0])]},
+            "bound": {"max_part_num": n_box, "objs": [
+                _obj("box", box_lo, box_hi, [1], [0, 0, 0], layers=3)]},
+        }
+        out.append((cfg, scen))
+    return out
