@@ -203,6 +203,7 @@ int bind_sets(tsph_ctx *c, const tsph_set *f, const tsph_set *b) {
     if (f->n != h.f_n || b->n != h.b_n) {
         h.f_n = f->n;
         h.b_n = b->n;
+        c->k.s0 = h;
         TSPH_CK(cudaMemcpy((void *)c->k.sc, c->host_sc, sizeof(SceneConst), cudaMemcpyHostToDevice));
     }
     return TSPH_OK;
@@ -320,7 +321,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     c.use_graph = 1;
 
     std::vector<SceneConst> sc(S);
-    long long cbase = 0, fslot = 0, bslot = 0, fuser = 0, buser = 0;
+    long long cbase = 0, fslot = 0, bslot = 0, fuser = 0, buser = 0, ublk = 0;
     int st_on = 0;
     for (int s = 0; s < S; ++s) {
         make_scene(ps[s], sc[s]);
@@ -337,7 +338,11 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
         sc[s].b_slots = round_chunk(batch ? nb : (capb > 0 ? capb : 1));
         fslot += sc[s].f_slots;
         bslot += sc[s].b_slots;
-        fuser += batch ? nf : capf;
+        const long long fu = batch ? nf : capf;
+        sc[s].f_ublk0 = ublk;
+        sc[s].f_ublks = fu > 0 ? (fu + kBlock - 1) / kBlock : 1;
+        ublk += sc[s].f_ublks;
+        fuser += fu;
         buser += batch ? nb : capb;
         if (ps[s].surface_tension_gamma != 0.f) st_on = 1;
     }
@@ -362,8 +367,10 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
 
     std::vector<int> fchunk(fcap / kChunk, 0), bchunk(bcap / kChunk, 0);
     std::vector<int> fus(fuser > 0 ? fuser : 1, 0), bus(buser > 0 ? buser : 1, 0);
+    std::vector<int> fub(ublk, 0);
     std::vector<long long> cb(S + 1);
     for (int s = 0; s < S; ++s) {
+        for (long long i = 0; i < sc[s].f_ublks; ++i) fub[sc[s].f_ublk0 + i] = s;
         for (long long i = sc[s].f_slot / kChunk; i < (sc[s].f_slot + sc[s].f_slots) / kChunk; ++i) fchunk[i] = s;
         for (long long i = sc[s].b_slot / kChunk; i < (sc[s].b_slot + sc[s].b_slots) / kChunk; ++i) bchunk[i] = s;
         const long long fu = batch ? sc[s].f_n : capf, bu = batch ? sc[s].b_n : capb;
@@ -421,7 +428,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     B.comp = A.get<float>(bcap);
     B.a2 = A.get<float>(bcap);
     B.alpha = A.get<float>(bcap);
-    c.S.partials_len = 2 * 8 * ((fcap + bcap) / kBlock) + 64;  // up to 8 threads per particle
+    c.S.partials_len = 2 * 8 * ((fcap + bcap) / kBlock) + 2 * ublk + 64;  // up to 8 threads per particle
     c.S.partials = A.get<double>(c.S.partials_len);
     const int64_t nscan = (nn + 4095) / 4096 + 1;
     c.S.scan_len = 2 * nscan;
@@ -435,12 +442,16 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     int *d_fus = A.get<int>((long long)fus.size());
     int *d_bus = A.get<int>((long long)bus.size());
     long long *d_cb = A.get<long long>(S + 1);
+    int *d_fub = A.get<int>(ublk);
     k.sc = d_sc;
     k.f_chunk_scene = d_fchunk;
     k.b_chunk_scene = d_bchunk;
     k.f_user_scene = d_fus;
     k.b_user_scene = d_bus;
     k.cbase_list = d_cb;
+    k.f_ublock_scene = d_fub;
+    k.f_ublocks = ublk;
+    k.s0 = sc[0];
     cudaError_t e = A.err;
     if (e == cudaSuccess) e = cudaMemcpy(d_sc, sc.data(), sizeof(SceneConst) * S, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_fchunk, fchunk.data(), sizeof(int) * fchunk.size(), cudaMemcpyHostToDevice);
@@ -448,6 +459,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     if (e == cudaSuccess) e = cudaMemcpy(d_fus, fus.data(), sizeof(int) * fus.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_bus, bus.data(), sizeof(int) * bus.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_cb, cb.data(), sizeof(long long) * (S + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_fub, fub.data(), sizeof(int) * ublk, cudaMemcpyHostToDevice);
     void *hp = nullptr;
     if (e == cudaSuccess) e = cudaMallocHost(&hp, sizeof(SceneConst) * S);
     if (e == cudaSuccess) {

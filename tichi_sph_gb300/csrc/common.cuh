@@ -45,6 +45,9 @@ struct SceneConst {
     // caller order [f_user, f_user + f_n); sorted slots [f_slot, f_slot + f_slots)
     long long f_user, f_n, f_slot, f_slots;
     long long b_user, b_n, b_slot, b_slots;
+    // blocks [f_ublk0, f_ublk0 + f_ublks) of kBlock caller-order fluid particles (at
+    // least one, so every scene has a block that finishes its step)
+    long long f_ublk0, f_ublks;
 };
 
 // Scalars of a scene that persist across steps.
@@ -96,7 +99,33 @@ struct KConst {
     const int *f_user_scene;              // scene of each caller-order particle
     const int *b_user_scene;
     const long long *cbase_list;          // cbase of every scene, then total_nodes
+    const int *f_ublock_scene;            // scene of each caller-order block of kBlock
+    long long f_ublocks;
+    SceneConst s0;                        // scene 0 by value (the one-scene kernels read it here)
 };
+
+// Scene lookups of a kernel instance.  A batched instance (M) finds its block's
+// scene in the chunk table and reads the scene's constants from the scene table;
+// a one-scene instance reads them from the launch's constant bank (no registers
+// held across the neighbour loops) and its grid scan positions are its sorted
+// slots (shift 0).
+template <bool M>
+__device__ __forceinline__ int f_block_scene(const KConst &k, int64_t first_slot) {
+    return M ? k.f_chunk_scene[first_slot / kChunk] : 0;
+}
+template <bool M>
+__device__ __forceinline__ int b_block_scene(const KConst &k, int64_t first_slot) {
+    return M ? k.b_chunk_scene[first_slot / kChunk] : 0;
+}
+template <bool M>
+__device__ __forceinline__ const SceneConst &scene(const KConst &k, int sc) {
+    if (M) return k.sc[sc];
+    return k.s0;
+}
+template <bool M>
+__device__ __forceinline__ long long shift_of(long long v) {
+    return M ? v : 0ll;
+}
 
 // The geometric constants a neighbour loop needs, in registers.
 struct Geo {
@@ -378,20 +407,23 @@ __device__ __forceinline__ void walk_blocks(const int *__restrict__ nbr, int64_t
 // candidate scan of the template cells.  Both visit the pairs the density sweep
 // selected; the callbacks keep their own 0 < r < h test, which is what selects
 // the pairs on the scanning path.
-template <int DIM, bool BOUND, int TPP, class FF, class FB>
-__device__ __forceinline__ void for_each_neighbor_tpp(const Geo &g, const FluidBuf &F, const BoundBuf &B,
-                                                      long long f_shift, long long b_shift, int64_t s, int q,
+template <int DIM, bool BOUND, int TPP, bool M, class FF, class FB>
+__device__ __forceinline__ void for_each_neighbor_tpp(const SceneConst &c, const SceneStep &st, int R,
+                                                      const FluidBuf &F, const BoundBuf &B, int64_t s, int q,
                                                       float4 pi, FF &&ff, FB &&fb) {
     const unsigned int pc = F.nbr_cnt[s];
     if (pc != kNbrOverflow) {
         const int nfl = (int)(pc & 0xffffu), nbo = (int)(pc >> 16);
         walk_blocks<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl, ff, fb);
     } else {
+        // the grid geometry and the scan shifts are loaded only on this (rare) path
+        Geo g;
+        g.load(c, R);
         bool ok;
         const long long code = cell_code<DIM>(pi, g, ok);
         if (ok) {
-            visit_candidates<DIM, TPP>(F.start, g, code, f_shift, q, ff);
-            if (BOUND) visit_candidates<DIM, TPP>(B.start, g, code, b_shift, q, fb);
+            visit_candidates<DIM, TPP>(F.start, g, code, shift_of<M>(st.f_shift), q, ff);
+            if (BOUND) visit_candidates<DIM, TPP>(B.start, g, code, shift_of<M>(st.b_shift), q, fb);
         }
     }
 }

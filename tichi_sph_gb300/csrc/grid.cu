@@ -297,21 +297,24 @@ __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, B
 
 // ----------------------------------------------------------------------------- update
 // SPH_update_volume_frac, SPH_update_mass, SPH_update_pos and SPH_update_energy
-// (sph.py:265-286, 375-379) in sorted order, writing the step's results back to
-// the caller's particle order.  Energies: per-particle FP32 terms, FP64 block
-// sums, the scene's blocks summed in order by the scene's last block.
+// (sph.py:265-286, 375-379) in the caller's particle order: each thread gathers
+// its particle's sorted state (inv) so that the ~20 per-particle result arrays
+// are written coalesced.  Blocks walk each scene's caller range padded to whole
+// blocks.  Energies: per-particle FP32 terms, FP64 block sums, the scene's
+// blocks summed in order by the scene's last block.
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, FluidBuf F,
                                                          const int *__restrict__ bstart, double *partials, int fbm,
                                                          int st_on) {
     __shared__ double sh[kBlock / 32];
-    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    const int sc = k.f_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
+    const int sc = k.f_ublock_scene[blockIdx.x];
     const SceneConst &c = k.sc[sc];
     SceneStep &st = k.ss[sc];
+    const int64_t local = (blockIdx.x - c.f_ublk0) * (int64_t)kBlock + threadIdx.x;
     double ke = 0.0, pe = 0.0;
-    if (s - c.f_slot < c.f_n) {
-        const int pid = F.perm[s];
+    if (local < c.f_n) {
+        const int64_t pid = c.f_user + local;
+        const int64_t s = F.inv[pid];
         const float dt = k.sp[sc].dt;
         const float4 v = F.vadv[st.cur * F.cap + s];
         const float4 p = F.pos[s];
@@ -323,8 +326,8 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
             if (fbm) {
                 const float t = F.vftmp[q * F.cap + s];
                 if (!flagged) vf += t;
-                U.volume_frac[(int64_t)pid * k.P + q] = vf;
-                U.volume_frac_tmp[(int64_t)pid * k.P + q] = t;
+                U.volume_frac[pid * k.P + q] = vf;
+                U.volume_frac_tmp[pid * k.P + q] = t;
             }
             rho0 += c.rho_phase[q] * vf;
         }
@@ -335,9 +338,7 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
         const float aa[3] = {acc.x, acc.y, acc.z};
         const float4 a1 = F.a1[s];
         const float a1v[3] = {a1.x, a1.y, a1.z};
-        const float4 nr = F.normal[s];
-        const float nrv[3] = {nr.x, nr.y, nr.z};
-        const int64_t b = (int64_t)pid * DIM;
+        const int64_t b = pid * DIM;
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
             U.pos[b + d] = np[d];
@@ -345,7 +346,12 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
             U.vel_adv[b + d] = vv[d];
             U.acce_adv[b + d] = aa[d];
             U.alpha_1[b + d] = a1v[d];
-            if (st_on) U.normal[b + d] = nrv[d];
+        }
+        if (st_on) {
+            const float4 nr = F.normal[s];
+            const float nrv[3] = {nr.x, nr.y, nr.z};
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) U.normal[b + d] = nrv[d];
         }
         if (fbm) {
             const float4 fa = F.facc[s];
@@ -356,7 +362,7 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
                 const float4 dv = F.drift[q * F.cap + s];
                 const float dvv[3] = {dv.x, dv.y, dv.z};
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) U.drift_vel[((int64_t)pid * k.P + q) * DIM + d] = dvv[d];
+                for (int d = 0; d < DIM; ++d) U.drift_vel[(pid * k.P + q) * DIM + d] = dvv[d];
             }
             U.fbm_zeta[pid] = F.zeta[s];
         }
@@ -386,9 +392,9 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
         partials[2 * blockIdx.x] = bke;
         partials[2 * blockIdx.x + 1] = bpe;
     }
-    const unsigned int nblk = (unsigned int)(c.f_slots / kBlock);
+    const unsigned int nblk = (unsigned int)c.f_ublks;
     if (last_block_done(&st.ticket[kStUpdate], nblk)) {
-        const int64_t b0 = c.f_slot / kBlock;
+        const int64_t b0 = c.f_ublk0;
         double a = 0.0, b = 0.0;
         for (int64_t i = threadIdx.x; i < (int64_t)nblk; i += kBlock) {
             a += __ldcg(partials + 2 * (b0 + i));
@@ -413,13 +419,12 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_update_bound(KConst k, tsph_set U, BoundBuf B,
                                                          const int *__restrict__ fstart) {
-    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= B.cap) return;
-    const int sc = k.b_chunk_scene[s / kChunk];
+    const int64_t pid = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (pid >= U.n) return;
+    const int sc = k.b_user_scene[pid];
     const SceneConst &c = k.sc[sc];
-    if (s - c.b_slot >= c.b_n) return;
     const SceneStep &st = k.ss[sc];
-    const int pid = B.perm[s];
+    const int64_t s = B.inv[pid];
     U.W[pid] = B.W[s];
     U.sph_density[pid] = B.rho[s];
     U.sph_compression[pid] = B.comp[s];
@@ -538,13 +543,15 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
 void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st) {
     const int fbm = c.p.fbm_enabled ? 1 : 0;
     const int st_on = c.st_on;
+    // boundary: over the caller's count (the kernel returns past it); one block at least
+    const int nbb = b.n > 0 ? blocks_for(b.n) : 1;
     c.launches += 2;
     if (c.k.dim == 3) {
-        k_update_fluid<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
-        k_update_bound<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
+        k_update_fluid<3><<<(int)c.k.f_ublocks, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
+        k_update_bound<3><<<nbb, kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
     } else {
-        k_update_fluid<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
-        k_update_bound<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
+        k_update_fluid<2><<<(int)c.k.f_ublocks, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
+        k_update_bound<2><<<nbb, kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
     }
 }
 

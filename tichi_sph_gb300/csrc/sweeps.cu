@@ -107,16 +107,16 @@ __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf 
     }
 }
 
-template <int DIM>
+template <int DIM, bool M>
 __global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    const int sc = k.f_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
-    const SceneConst &c = k.sc[sc];
+    const int sc = f_block_scene<M>(k, blockIdx.x * (int64_t)kBlock);
+    const SceneConst &c = scene<M>(k, sc);
     if (s - c.f_slot >= c.f_n) return;
     const SceneStep &st = k.ss[sc];
     Geo g;
     g.load(c, k.R);
-    const long long f_shift = st.f_shift, b_shift = st.b_shift;
+    const long long f_shift = shift_of<M>(st.f_shift), b_shift = shift_of<M>(st.b_shift);
     const float4 pi = F.pos[s];
     bool ok;
     const long long code = cell_code<DIM>(pi, g, ok);
@@ -192,11 +192,11 @@ __global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf 
 
 // The boundary's own sums: SPH_prepare_attr (b,b)(b,f), SPH_prepare_alpha_2 (b,f),
 // SPH_prepare_alpha (sph.py:50-105 as called by main.py:190-197).
-template <int DIM>
+template <int DIM, bool M>
 __global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    const int sc = k.b_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
-    const SceneConst &c = k.sc[sc];
+    const int sc = b_block_scene<M>(k, blockIdx.x * (int64_t)kBlock);
+    const SceneConst &c = scene<M>(k, sc);
     if (s - c.b_slot >= c.b_n) return;
     const SceneStep &st = k.ss[sc];
     Geo g;
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, 
     const long long code = cell_code<DIM>(pi, g, ok);
     float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f;
     if (ok) {
-        visit_candidates<DIM>(B.start, g, code, st.b_shift, 0, [&](int j) {
+        visit_candidates<DIM>(B.start, g, code, shift_of<M>(st.b_shift), 0, [&](int j) {
             const float4 pj = B.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, 
                 comp += w * mv.y;
             }
         });
-        visit_candidates<DIM>(F.start, g, code, st.f_shift, 0, [&](int j) {
+        visit_candidates<DIM>(F.start, g, code, shift_of<M>(st.f_shift), 0, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
@@ -295,17 +295,17 @@ __global__ void k_solve_begin(KConst k, int kind, int flip, cudaGraphConditional
 // psi_adv / alpha; the scene's sum of psi_adv / psi0 goes to per-block partials
 // and, through the scene's last block, to its psi_sum (block order:
 // deterministic).
-template <int DIM, int TPP>
+template <int DIM, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B, double *partials) {
     __shared__ double sh[kBlock / 32];
     __shared__ unsigned int arrived;
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
-    const int sc = k.f_chunk_scene[first / kChunk];
+    const int sc = f_block_scene<M>(k, first);
     SceneStep &st = k.ss[sc];
     if (!st.cond) return;  // this scene's loop has ended (uniform over the block)
     if (threadIdx.x == 0) arrived = 0;
     __syncthreads();
-    const SceneConst &c = k.sc[sc];
+    const SceneConst &c = scene<M>(k, sc);
     const Lanes<TPP> ln;
     const int64_t s = ln.s;
     const bool act = s - c.f_slot < c.f_n;
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B
     if (act) {
         pi = F.pos[s];
         vi = vin[s];
-        for_each_neighbor_tpp<DIM, true, TPP>(g, F, B, st.f_shift, st.b_shift, s, ln.q, pi,
+        for_each_neighbor_tpp<DIM, true, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
             [&](int j) {
                 const float4 pj = F.pos[j];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -373,16 +373,16 @@ __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B
 // v_adv buffer, TPP threads per particle.  The scene's last block evaluates the
 // loop test of main.py:201-213 / 222-234 from sweep A's sum; the grid's last
 // block sets the graph's while-node condition.
-template <int DIM, int TPP>
+template <int DIM, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B, int kind,
                                                 cudaGraphConditionalHandle h, int use_cond) {
     __shared__ unsigned int arrived;
     if (threadIdx.x == 0) arrived = 0;
     __syncthreads();
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
-    const int sc = k.f_chunk_scene[first / kChunk];
+    const int sc = f_block_scene<M>(k, first);
     SceneStep &st = k.ss[sc];
-    const SceneConst &c = k.sc[sc];
+    const SceneConst &c = scene<M>(k, sc);
     const bool running = st.cond != 0;
     if (running) {
         const Lanes<TPP> ln;
@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
             const float4 pi = F.pos[s];
             const float ki = F.kappa[s];
             const float Xi = pi.w;
-            for_each_neighbor_tpp<DIM, true, TPP>(g, F, B, st.f_shift, st.b_shift, s, ln.q, pi,
+            for_each_neighbor_tpp<DIM, true, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
                 [&](int j) {
                     const float4 pj = F.pos[j];
                     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -463,11 +463,11 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
 
 // ----------------------------------------------------------------------------- advection
 // First pass of SPH_advection_surface_tension_acc, sph.py:134-150: surface normals.
-template <int DIM, int TPP>
+template <int DIM, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
-    const int sc = k.f_chunk_scene[first / kChunk];
-    const SceneConst &c = k.sc[sc];
+    const int sc = f_block_scene<M>(k, first);
+    const SceneConst &c = scene<M>(k, sc);
     const SceneStep &st = k.ss[sc];
     const Lanes<TPP> ln;
     const int64_t s = ln.s;
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
     float nx = 0.f, ny = 0.f, nz = 0.f;
     if (act) {
         const float4 pi = F.pos[s];
-        for_each_neighbor_tpp<DIM, false, TPP>(g, F, B, st.f_shift, st.b_shift, s, ln.q, pi,
+        for_each_neighbor_tpp<DIM, false, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
             [&](int j) {
                 const float4 pj = F.pos[j];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -504,11 +504,11 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
 // kernel weight, so -- like the reference -- it runs over every candidate in the
 // template cells, not only those within h: with surface tension on this sweep
 // scans the cells; without it, it walks the neighbour list.
-template <int DIM, bool ST, int TPP>
+template <int DIM, bool ST, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
-    const int sc = k.f_chunk_scene[first / kChunk];
-    const SceneConst &c = k.sc[sc];
+    const int sc = f_block_scene<M>(k, first);
+    const SceneConst &c = scene<M>(k, sc);
     const SceneStep &st = k.ss[sc];
     const Lanes<TPP> ln;
     const int64_t s = ln.s;
@@ -562,9 +562,9 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
         if (ST) {
             bool ok;
             const long long code = cell_code<DIM>(pi, g, ok);
-            if (ok) visit_candidates<DIM, TPP>(F.start, g, code, st.f_shift, ln.q, pair);
+            if (ok) visit_candidates<DIM, TPP>(F.start, g, code, shift_of<M>(st.f_shift), ln.q, pair);
         } else {
-            for_each_neighbor_tpp<DIM, false, TPP>(g, F, B, st.f_shift, st.b_shift, s, ln.q, pi, pair,
+            for_each_neighbor_tpp<DIM, false, TPP, M>(c, st, k.R, F, B, s, ln.q, pi, pair,
                                                    [&](int) {});
         }
     }
@@ -590,15 +590,21 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
 }
 
 // ----------------------------------------------------------------------------- launchers
+// One-scene (M = false) or batched (M = true) kernel instances.
+#define TSPH_M_DISPATCH(MULTI, ...)                                       \
+    if (MULTI) { constexpr bool M = true; __VA_ARGS__; }                   \
+    else { constexpr bool M = false; __VA_ARGS__; }
+
 void launch_density(tsph_ctx &c, cudaStream_t st) {
     c.launches += 2;
-    if (c.k.dim == 3) {
-        k_density_fluid<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
-        k_density_bound<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
-    } else {
-        k_density_fluid<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
-        k_density_bound<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
-    }
+    TSPH_M_DISPATCH(c.n_scenes > 1,
+        if (c.k.dim == 3) {
+            k_density_fluid<3, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+            k_density_bound<3, M><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+        } else {
+            k_density_fluid<2, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+            k_density_bound<2, M><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+        })
 }
 
 void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
@@ -621,18 +627,18 @@ void launch_psi(tsph_ctx &c, cudaStream_t st) {
     c.launches += 1;
     const int tpp = c.tpp;
     const int nb = tpp_blocks(c.F.cap, tpp);
-    TSPH_TPP_DISPATCH(tpp,
-        if (c.k.dim == 3) k_psi<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
-        else k_psi<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials));
+    TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
+        if (c.k.dim == 3) k_psi<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
+        else k_psi<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials)))
 }
 
 void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
     c.launches += 1;
     const int tpp = c.tpp;
     const int nb = tpp_blocks(c.F.cap, tpp);
-    TSPH_TPP_DISPATCH(tpp,
-        if (c.k.dim == 3) k_vel<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond);
-        else k_vel<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond));
+    TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
+        if (c.k.dim == 3) k_vel<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond);
+        else k_vel<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond)))
 }
 
 void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
@@ -645,22 +651,22 @@ void launch_advect(tsph_ctx &c, cudaStream_t st) {
     const int nb = tpp_blocks(c.F.cap, tpp);
     const bool st_on = c.st_on != 0;
     c.launches += st_on ? 2 : 1;
-    TSPH_TPP_DISPATCH(tpp,
+    TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
         if (c.k.dim == 3) {
             if (st_on) {
-                k_normal<3, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
-                k_advect<3, true, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_normal<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<3, true, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
             } else {
-                k_advect<3, false, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<3, false, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
             }
         } else {
             if (st_on) {
-                k_normal<2, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
-                k_advect<2, true, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_normal<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<2, true, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
             } else {
-                k_advect<2, false, TPP><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<2, false, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
             }
-        });
+        }))
 }
 
 }  // namespace tsph
