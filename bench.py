@@ -311,6 +311,67 @@ def other_line(res, args, ws):
                        "min_volume_fraction": res["vf_min"]}}
 
 
+def run_adjoint(reps, warmup, dev, substeps=64, checkpoint_every=8):
+    """Config of the differentiable form: a 99,452-particle block, 64 substeps at
+    dt 5e-4, loss = |centre of mass - target|^2 + 0.1 mean density error^2,
+    gradients with respect to the initial velocities and the viscosity.  Times
+    the forward (rollout + final density) and the backward (recompute of every
+    checkpoint segment but the last + the reverse sweeps) with CUDA events."""
+    import torch
+    from tichi_sph_gb300 import sph_config, workloads
+    from tichi_sph_gb300.adjoint import DiffRollout, com_density_loss
+    from tichi_sph_gb300.simulation import Simulation
+    c, sc_, vel, target = workloads.diff_block()
+    cfg = sph_config.Config(c, sc_)
+    sim = Simulation(cfg, device=dev)
+    sim.init_scenario()
+    n = sim.fluid.part_num[None]
+    roll = DiffRollout(cfg, sim.fluid, sim.bound, substeps, checkpoint_every=checkpoint_every)
+    v0 = torch.as_tensor(vel(n), device=dev)
+    tgt = torch.as_tensor(target, device=dev)
+    mass = sim.fluid.mass[:n].double()
+    rho0 = sim.fluid.rest_density[:n].double()
+    stream = torch.cuda.current_stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fw, bw, gnorm, gmu, loss = [], [], 0.0, 0.0, 0.0
+    for r in range(warmup + reps):
+        v = v0.clone().requires_grad_(True)
+        mu = torch.tensor(0.01, dtype=torch.float64, requires_grad=True)
+        torch.cuda.synchronize(dev)
+        ev[0].record(stream)
+        x, _, rho = roll(v, mu)
+        L = com_density_loss(x.double(), rho.double(), mass, rho0, tgt)
+        ev[1].record(stream)
+        L.backward()
+        ev[2].record(stream)
+        torch.cuda.synchronize(dev)
+        if r >= warmup:
+            fw.append(ev[0].elapsed_time(ev[1]))
+            bw.append(ev[1].elapsed_time(ev[2]))
+        gnorm, gmu, loss = float(v.grad.norm()), float(mu.grad), float(L)
+    st = roll.solver.stats()
+    roll.close()
+    fwm, bwm = sum(fw) / len(fw), sum(bw) / len(bw)
+    return {"n": n, "nb": sim.bound.part_num[None], "substeps": substeps, "checkpoint_every": checkpoint_every,
+            "forward_ms": fwm, "backward_ms": bwm, "ratio": bwm / fwm, "grad_v_norm": gnorm, "grad_mu": gmu,
+            "loss": loss, "reps": reps, "warmup": warmup, "last_div_iter": st["div_iter"],
+            "last_incom_iter": st["incom_iter"]}
+
+
+def adjoint_line(res, args, ws):
+    return {"metric": "backward/forward time", "value": res["ratio"], "unit": "ratio", "n_gpus": ws,
+            "steps": res["reps"], "warmup": res["warmup"], "ms_per_step": res["forward_ms"] + res["backward_ms"],
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "differentiable DFSPH: %d-particle block (46 x 46 x 47 at 0.01 m) in a 3-layer "
+                                   "tank (%d boundary), %d substeps at dt 5e-4, checkpoint every %d; loss |CoM - "
+                                   "target|^2 + 0.1 mean((rho - rho0) / rho0)^2; d/d(initial velocities), d/d(mu)"
+                                   % (res["n"], res["nb"], res["substeps"], res["checkpoint_every"]),
+                       "forward_ms": res["forward_ms"], "backward_ms": res["backward_ms"],
+                       "forward_particle_steps_per_s": res["n"] * res["substeps"] / (res["forward_ms"] / 1e3),
+                       "loss": res["loss"], "grad_v_norm": res["grad_v_norm"], "grad_mu": res["grad_mu"],
+                       "last_div_iter": res["last_div_iter"], "last_incom_iter": res["last_incom_iter"]}}
+
+
 def run_reference(args, rank, ws):
     if rank != 0:
         return 0
@@ -348,7 +409,8 @@ def main():
                          "as profilers list them)")
     ap.add_argument("--no-profile", action="store_true", help="skip the per-phase timing (roofline)")
     ap.add_argument("--tpp", type=int, default=0, help="threads per particle (0: autotune after warm-up)")
-    ap.add_argument("--workload", default="dambreak3d", choices=["dambreak3d", "batched", "twophase3d", "dambreak2d"],
+    ap.add_argument("--workload", default="dambreak3d",
+                    choices=["dambreak3d", "batched", "twophase3d", "dambreak2d", "adjoint"],
                     help="dambreak3d: the headline line; the others print their own line")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched measurement added to the headline line (0: skip)")
@@ -370,6 +432,13 @@ def main():
         res = run_batched(256, args.steps, args.warmup, dev)
         if rank == 0:
             print(json.dumps(batched_line(res, args, ws)), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    if args.workload == "adjoint":
+        res = run_adjoint(args.steps, args.warmup, dev)
+        if rank == 0:
+            print(json.dumps(adjoint_line(res, args, ws)), flush=True)
         if dist:
             dist.destroy_process_group()
         return 0

@@ -216,6 +216,65 @@ int tsph_fluid_density_noalloc(const tsph_params *params, const float *fluid_pos
                                const float *bound_mass, const float *bound_rest_volume, int64_t n_bound,
                                float *W, float *sph_density, float *sph_compression, void *stream);
 
+/* ---------------------------------------------------------------- adjoint
+ * Hand-written reverse mode of the substep (no counterpart in the reference,
+ * which has no autodiff; the forward it reverses is tsph_substep, i.e. the
+ * substep of main.py:347-352 around sph_step, main.py:175-256).  Supported for
+ * a single-scene DFSPH context without surface tension or volume-fraction
+ * update.  Differentiable inputs: fluid positions and velocities at the start
+ * of the substep and the dynamic viscosity.  Held fixed: masses, rest
+ * densities, the boundary, dt, the iteration counts of the two Jacobi solves
+ * (those the forward took) and the neighbour pairs of the substep (the
+ * topology found at its start).  The clamps psi_adv = max(., 0) and
+ * alpha = max(., 1e-4) are differentiated one-sided.
+ *
+ * A tape holds `slots` recorded substeps (or density evaluations) with at most
+ * `max_iters` iterations per Jacobi solve.  Recording writes what the reverse
+ * sweeps need -- the sorted order, positions, neighbour lists, density and
+ * alpha terms, every Jacobi iterate -- into device memory owned by the tape;
+ * the reverse pass reads only the tape.  The caller arranges checkpointing. */
+typedef struct tsph_tape tsph_tape;
+
+enum {
+    TSPH_TAPE_ITER_OVERFLOW = 1,   /* a solve ran more than max_iters iterations */
+    TSPH_TAPE_LIST_OVERFLOW = 2,   /* a particle had more neighbours than its list holds */
+    TSPH_TAPE_OUTSIDE_GRID = 4,    /* a fluid particle had no valid cell (one-sided pairs) */
+    TSPH_TAPE_BOUND_PSI = 8        /* the boundary's psi_adv was nonzero */
+};
+
+int tsph_tape_create(tsph_ctx *ctx, int slots, int max_iters, tsph_tape **out);
+int tsph_tape_destroy(tsph_tape *tape);
+
+/* tsph_substep that also records into tape slot `slot`. */
+int tsph_substep_record(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, tsph_tape *tape, int slot,
+                        void *stream);
+
+/* Density of every fluid particle at the current positions (the grid build
+ * and density sweep of sph_step, sph.py:50-64), written to sph_density_out
+ * (caller order, device) and recorded into tape slot `slot`.  Changes no
+ * particle field. */
+int tsph_density_record(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, tsph_tape *tape, int slot,
+                        float *sph_density_out, void *stream);
+
+/* Reverse of the substep recorded in `slot`: from dL/dpos and dL/dvel after it
+ * (caller order, [n][dim], device FP32) writes dL/dpos and dL/dvel before it
+ * (may alias the inputs) and adds dL/dviscosity to *grad_viscosity (one
+ * device double).  Synchronises once per tape recording to read the slots'
+ * iteration counts; returns TSPH_ERR_STATE with the slot's TSPH_TAPE_* bits in
+ * the error text when the recording cannot be reversed. */
+int tsph_substep_adjoint(tsph_ctx *ctx, tsph_tape *tape, int slot, const float *grad_pos_out,
+                         const float *grad_vel_out, float *grad_pos_in, float *grad_vel_in, double *grad_viscosity,
+                         void *stream);
+
+/* Reverse of the density evaluation recorded in `slot`: adds dL/dpos to
+ * grad_pos ([n][dim]) from dL/dsph_density ([n]); caller order, device. */
+int tsph_density_adjoint(tsph_ctx *ctx, tsph_tape *tape, int slot, const float *grad_density, float *grad_pos,
+                         void *stream);
+
+/* Sets the dynamic viscosity of scene `scene` (global_dynamic_viscosity,
+ * sph_config.py:149) for the following steps. */
+int tsph_set_viscosity(tsph_ctx *ctx, int scene, float viscosity);
+
 /* Library version string. */
 const char *tsph_version(void);
 

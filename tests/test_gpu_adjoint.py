@@ -1,0 +1,134 @@
+"""The hand-written CUDA adjoint against the FP64 oracle (needs a GPU).
+
+Workload: the differentiable dam-block scene at 2,028 particles (13 x 12 x 13)
+in its tank, 16 substeps at dt = 5e-4 with both solves fixed at two iterations,
+loss = |centre of mass - target|^2 + 0.1 mean(((rho - rho0) / rho0)^2),
+gradients with respect to the initial velocity field and the viscosity.  The
+reference values are FP64: torch.autograd through the autodiff oracle and
+central finite differences of the oracle's forward.  Bar: 1e-3 relative.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _need_cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+STEPS = 16
+
+
+def _setup(steps=STEPS, K=8, nx=13, ny=12, nz=13, fixed_iters=2):
+    from oracle import sph_autodiff as A
+    from oracle import sph_oracle as O
+    from tichi_sph_gb300 import sph_config, workloads
+    from tichi_sph_gb300.adjoint import DiffRollout
+    from tichi_sph_gb300.simulation import Simulation
+    c, s, vel, target = workloads.diff_block(nx=nx, ny=ny, nz=nz, fixed_iters=fixed_iters)
+    cfg = sph_config.Config(c, s)
+    sim = Simulation(cfg, device="cuda")
+    sim.init_scenario()
+    nf, nb = sim.fluid.part_num[None], sim.bound.part_num[None]
+    roll = DiffRollout(cfg, sim.fluid, sim.bound, steps, checkpoint_every=K)
+    v0 = vel(nf)
+    p = O.Params.from_config(c, s, taichi_f32=True)
+    dt = float(np.float32(np.float32(p.part_size) / np.float32(p.cs)))
+    f64 = lambda t: t.detach().cpu().numpy().astype(np.float64)
+    sc = A.Scene(3, p.h, p.sig, f64(sim.fluid.mass[:nf]), f64(sim.fluid.rest_density[:nf]),
+                 f64(sim.bound.pos[:nb]), f64(sim.bound.mass[:nb]), p.gravity, dt)
+    x0 = torch.as_tensor(f64(sim.fluid.pos[:nf]))
+    return sim, roll, v0, target, sc, x0, p
+
+
+def _cuda_grad(sim, roll, v0, target, mu=0.01):
+    from tichi_sph_gb300.adjoint import com_density_loss
+    n = roll.n
+    v = torch.as_tensor(v0, dtype=torch.float64, device="cuda").requires_grad_(True)
+    m = torch.tensor(mu, dtype=torch.float64, requires_grad=True)
+    x, _, rho = roll(v, m)
+    L = com_density_loss(x.double(), rho.double(), sim.fluid.mass[:n].double(), sim.fluid.rest_density[:n].double(),
+                         torch.as_tensor(target, device="cuda"))
+    L.backward()
+    return float(L), v.grad.detach().cpu().double(), float(m.grad), x.detach().cpu().double()
+
+
+def _ref_loss(sc, x0, v0, mu, target, steps=STEPS):
+    from oracle import sph_autodiff as A
+    x, comp = x0, 0.0
+    v = v0
+    for _ in range(steps):
+        x, v, comp, _ = A.substep(sc, x, v, mu, comp, iters=(2, 2))
+    return A.loss_fn(sc, x, torch.as_tensor(target, dtype=A.T)), x
+
+
+def test_adjoint_matches_fp64_autograd_and_fd():
+    _need_cuda()
+    sim, roll, v0, target, sc, x0, p = _setup()
+    L, gv, gmu, xT = _cuda_grad(sim, roll, v0, target)
+    roll.close()
+    # FP64 autograd through the oracle
+    v = torch.as_tensor(v0, dtype=torch.float64).requires_grad_(True)
+    m = torch.tensor(0.01, dtype=torch.float64, requires_grad=True)
+    Lr, xr = _ref_loss(sc, x0, v, m, target)
+    Lr.backward()
+    assert float((xT - xr.detach()).abs().max()) < 2e-6          # forward: FP32 vs FP64 trajectories
+    assert abs(L - float(Lr)) <= 1e-4 * abs(float(Lr))
+    rel_v = float((gv - v.grad).norm() / v.grad.norm())
+    rel_mu = abs(gmu - float(m.grad)) / abs(float(m.grad))
+    assert rel_v < 1e-3, rel_v
+    assert rel_mu < 1e-3, rel_mu
+    # FP64 central differences of the oracle's forward
+    h = 1e-6
+    d = torch.as_tensor(np.random.default_rng(11).standard_normal(tuple(v.shape)))
+    with torch.no_grad():
+        vv = torch.as_tensor(v0, dtype=torch.float64)
+        mm = torch.tensor(0.01, dtype=torch.float64)
+        fd_mu = float(_ref_loss(sc, x0, vv, mm + h, target)[0] - _ref_loss(sc, x0, vv, mm - h, target)[0]) / (2 * h)
+        fd_v = float(_ref_loss(sc, x0, vv + h * d, mm, target)[0] - _ref_loss(sc, x0, vv - h * d, mm, target)[0]) / (2 * h)
+    assert abs(gmu - fd_mu) <= 1e-3 * abs(fd_mu)
+    assert abs(float((gv * d).sum()) - fd_v) <= 1e-3 * abs(fd_v)
+
+
+def test_checkpoint_interval_does_not_change_gradients():
+    _need_cuda()
+    out = []
+    for K in (3, 8, STEPS):
+        sim, roll, v0, target, _, _, _ = _setup(K=K)
+        out.append(_cuda_grad(sim, roll, v0, target))
+        roll.close()
+    for o in out[1:]:
+        assert o[0] == out[0][0]
+        assert torch.equal(o[1], out[0][1])
+        assert o[2] == out[0][2]
+
+
+def test_adjoint_with_convergence_tolerances():
+    """Solver loops on their tolerances (the workload's own 1% / 0.1%): the
+    recorded iteration counts drive the reverse sweeps; the gradients are finite."""
+    _need_cuda()
+    sim, roll, v0, target, sc, x0, p = _setup(fixed_iters=None, steps=8)
+    L, gv, gmu, xT = _cuda_grad(sim, roll, v0, target)
+    roll.close()
+    assert np.isfinite(L) and torch.isfinite(gv).all() and np.isfinite(gmu)
+
+
+def test_tape_rejects_unsupported_contexts():
+    _need_cuda()
+    import ctypes as C
+    from tichi_sph_gb300 import _native, Solver, sph_config
+    from tichi_sph_gb300.simulation import Simulation
+    from tests import golden_io as G
+    import json
+    cpath, spath = G.paths("vfsph2d")
+    cfg = sph_config.Config(json.load(open(cpath)), json.load(open(spath)))
+    sim = Simulation(cfg, device="cuda")
+    sim.init_scenario()
+    s = Solver(cfg, sim.fluid, sim.bound)
+    tape = C.c_void_p()
+    rc = _native.lib().tsph_tape_create(s.ctx, 2, 4, C.byref(tape))
+    assert rc == _native.ERR_INVALID
+    s.close()

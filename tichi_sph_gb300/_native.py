@@ -86,6 +86,15 @@ SIGNATURES = {
     "tsph_profile_phases": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_int, _fp, C.c_void_p]),
     "tsph_fluid_density_noalloc": (C.c_int, [C.POINTER(Params), _fp, _fp, _fp, _i64, _fp, _fp, _fp, _i64,
                                              _fp, _fp, _fp, C.c_void_p]),
+    "tsph_tape_create": (C.c_int, [CtxP, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "tsph_tape_destroy": (C.c_int, [C.c_void_p]),
+    "tsph_substep_record": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p, C.c_int, C.c_void_p]),
+    "tsph_density_record": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p, C.c_int, _fp,
+                                      C.c_void_p]),
+    "tsph_substep_adjoint": (C.c_int, [CtxP, C.c_void_p, C.c_int, _fp, _fp, _fp, _fp,
+                                       C.POINTER(C.c_double), C.c_void_p]),
+    "tsph_density_adjoint": (C.c_int, [CtxP, C.c_void_p, C.c_int, _fp, _fp, C.c_void_p]),
+    "tsph_set_viscosity": (C.c_int, [CtxP, C.c_int, C.c_float]),
     "tsph_version": (C.c_char_p, []),
     "tsph_last_error": (C.c_char_p, []),
 }

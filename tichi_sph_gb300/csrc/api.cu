@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "ctx.h"
+#include "tape.h"
 
 using namespace tsph;
 
@@ -134,7 +135,16 @@ int solve(tsph_ctx &c, int kind, cudaStream_t st, bool graph) {
     return while_loop(
         c, st, graph, &c.k.dg->cond_any, &c.host_dg->cond_any,
         [&](cudaGraphConditionalHandle h, int u, cudaStream_t s) { launch_solve_begin(c, kind, h, u, s); },
-        [&](cudaGraphConditionalHandle h, int u, cudaStream_t s) { launch_solve_iter(c, kind, h, u, s); });
+        [&](cudaGraphConditionalHandle h, int u, cudaStream_t s) {
+            if (c.rec_tape) {
+                // record the iterate and kappa between the two sweeps
+                launch_psi(c, s);
+                launch_tape_iter(c, kind, s);
+                launch_vel(c, kind, h, u, s);
+            } else {
+                launch_solve_iter(c, kind, h, u, s);
+            }
+        });
 }
 
 int fbm_loop(tsph_ctx &c, cudaStream_t st, bool graph) {
@@ -151,18 +161,29 @@ int enqueue_step(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t
     if (with_cfl) launch_cfl(c, f, st);
     launch_grid_build(c, f, b, st);
     launch_density(c, st);
+    if (c.rec_tape) launch_tape_state(c, st);
     int rc = solve(c, kSolveDiv, st, graph);
     if (rc) return rc;
     launch_advect(c, st);
+    if (c.rec_tape) launch_tape_vmid(c, st);
     rc = solve(c, kSolveDens, st, graph);
     if (rc) return rc;
     if (c.p.fbm_enabled) {
         rc = fbm_loop(c, st, graph);
         if (rc) return rc;
     }
+    if (c.rec_tape) launch_tape_end(c, st);
     launch_unsort(c, f, b, st);
     c.launches_per_step = c.launches;
     return TSPH_OK;
+}
+
+// Cached graphs bake the launch-time constants in: any change of those drops them.
+void drop_graphs(tsph_ctx *c) {
+    for (int i = 0; i < 2; ++i) {
+        if (c->exec[i]) cudaGraphExecDestroy(c->exec[i]);
+        c->exec[i] = nullptr;
+    }
 }
 
 unsigned long long mix(unsigned long long h, unsigned long long v) {
@@ -222,10 +243,13 @@ int run_step(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream, bo
     }
     unsigned long long key[4];
     set_key(*f, *b, with_cfl ? 1 : 0, key);
-    if (!c->exec || std::memcmp(key, c->graph_key, sizeof(key)) != 0) {
-        if (c->exec) {
-            cudaGraphExecDestroy(c->exec);
-            c->exec = nullptr;
+    key[3] = mix(key[3], (unsigned long long)(uintptr_t)c->rec_tape);
+    const int gi = c->rec_tape ? 1 : 0;
+    cudaGraphExec_t &exec = c->exec[gi];
+    if (!exec || std::memcmp(key, c->graph_key[gi], sizeof(key)) != 0) {
+        if (exec) {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
         }
         cudaStream_t cap = extra(c)->cap_stream;
         TSPH_CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
@@ -237,15 +261,15 @@ int run_step(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream, bo
             return rc;
         }
         if (e != cudaSuccess) return fail_cuda(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&c->exec, graph, 0);
+        e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
-            c->exec = nullptr;
+            exec = nullptr;
             return fail_cuda(e, "cudaGraphInstantiate");
         }
-        std::memcpy(c->graph_key, key, sizeof(key));
+        std::memcpy(c->graph_key[gi], key, sizeof(key));
     }
-    TSPH_CK(cudaGraphLaunch(c->exec, st));
+    TSPH_CK(cudaGraphLaunch(exec, st));
     c->stepped++;
     return TSPH_OK;
 }
@@ -554,7 +578,7 @@ int tsph_create_batch(const tsph_params *scenes, int n_scenes, const int64_t *fl
 int tsph_destroy(tsph_ctx *c) {
     if (!c) return TSPH_OK;
     CtxBox *box = reinterpret_cast<CtxBox *>(c);
-    if (c->exec) cudaGraphExecDestroy(c->exec);
+    drop_graphs(c);
     for (void *p : box->x.alloc.ptrs) cudaFree(p);
     for (void *p : box->x.pinned) cudaFreeHost(p);
     if (box->x.cap_stream) cudaStreamDestroy(box->x.cap_stream);
@@ -573,10 +597,7 @@ int tsph_set_threads_per_particle(tsph_ctx *c, int tpp) {
     if (!c) return fail(TSPH_ERR_INVALID, "null ctx");
     if (tpp != 1 && tpp != 2 && tpp != 4 && tpp != 8)
         return fail(TSPH_ERR_INVALID, "threads per particle must be 1, 2, 4 or 8");
-    if (tpp != c->tpp && c->exec) {
-        cudaGraphExecDestroy(c->exec);
-        c->exec = nullptr;
-    }
+    if (tpp != c->tpp) drop_graphs(c);
     c->tpp = tpp;
     return TSPH_OK;
 }
@@ -667,6 +688,50 @@ int tsph_set_state(tsph_ctx *c, double time_count, float dt, double compression,
     if (!c) return fail(TSPH_ERR_INVALID, "null ctx");
     k_set_state<<<(c->n_scenes + 127) / 128, 128, 0, (cudaStream_t)stream>>>(c->k, time_count, dt, compression);
     TSPH_CK(cudaGetLastError());
+    return TSPH_OK;
+}
+
+int tsph_substep_record(tsph_ctx *c, const tsph_set *f, const tsph_set *b, tsph_tape *t, int slot, void *stream) {
+    if (!c || !t || t->ctx != c) return fail(TSPH_ERR_INVALID, "tape does not belong to this context");
+    if (slot < 0 || slot >= t->a.slots) return fail(TSPH_ERR_INVALID, "tape slot out of range");
+    int rc = tape_begin(*t, slot, (cudaStream_t)stream);
+    if (rc) return rc;
+    c->rec_tape = t;
+    rc = run_step(c, f, b, stream, true);
+    c->rec_tape = nullptr;
+    return rc;
+}
+
+int tsph_density_record(tsph_ctx *c, const tsph_set *f, const tsph_set *b, tsph_tape *t, int slot, float *out,
+                        void *stream) {
+    if (!c || !t || t->ctx != c) return fail(TSPH_ERR_INVALID, "tape does not belong to this context");
+    if (slot < 0 || slot >= t->a.slots) return fail(TSPH_ERR_INVALID, "tape slot out of range");
+    if (!out) return fail(TSPH_ERR_INVALID, "null output");
+    int rc = bind_sets(c, f, b);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = tape_begin(*t, slot, st);
+    if (rc) return rc;
+    c->rec_tape = t;
+    launch_step_begin(*c, st);
+    launch_grid_build(*c, *f, *b, st);
+    launch_density(*c, st);
+    launch_tape_state(*c, st);
+    c->rec_tape = nullptr;
+    launch_density_out(*c, out, st);
+    TSPH_CK(cudaGetLastError());
+    return TSPH_OK;
+}
+
+int tsph_set_viscosity(tsph_ctx *c, int scene, float viscosity) {
+    if (!c) return fail(TSPH_ERR_INVALID, "null ctx");
+    if (scene < 0 || scene >= c->n_scenes) return fail(TSPH_ERR_INVALID, "scene out of range");
+    SceneConst &h = c->host_sc[scene];
+    if (h.mu == viscosity) return TSPH_OK;
+    h.mu = viscosity;
+    if (scene == 0) c->k.s0.mu = viscosity;
+    TSPH_CK(cudaMemcpy((void *)(c->k.sc + scene), &h, sizeof(SceneConst), cudaMemcpyHostToDevice));
+    drop_graphs(c);  // the one-scene kernels read mu from the launch's constant bank
     return TSPH_OK;
 }
 

@@ -20,9 +20,11 @@ struct tsph_ctx {
     int st_on;                // some scene has surface tension
     int use_graph;
     int stepped;
-    // cached per-substep graph, keyed on the particle counts and array pointers
-    cudaGraphExec_t exec;
-    unsigned long long graph_key[4];
+    // cached per-substep graphs (plain, recording), keyed on the particle counts,
+    // array pointers and the recording tape
+    cudaGraphExec_t exec[2];
+    unsigned long long graph_key[2][4];
+    tsph_tape *rec_tape;      // non-null while a recorded step is enqueued
     int launches;             // kernel launches enqueued (counted by the launchers)
     int launches_per_step;    // top-level kernels of the last enqueued step
     int tpp;                  // threads per particle of the list sweeps (1, 2, 4, 8)
@@ -46,6 +48,14 @@ void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int 
 void launch_psi(tsph_ctx &c, cudaStream_t st);
 void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
 void launch_advect(tsph_ctx &c, cudaStream_t st);
+
+// adjoint.cu: recording hooks of the forward step
+void launch_tape_state(tsph_ctx &c, cudaStream_t st);
+void launch_tape_iter(tsph_ctx &c, int kind, cudaStream_t st);
+void launch_tape_vmid(tsph_ctx &c, cudaStream_t st);
+void launch_tape_end(tsph_ctx &c, cudaStream_t st);
+int tape_begin(tsph_tape &t, int slot, cudaStream_t st);
+void launch_density_out(tsph_ctx &c, float *out, cudaStream_t st);
 
 // fbm.cu
 void launch_fbm_begin(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);

@@ -134,3 +134,43 @@ def batched_dambreaks(n_scenes=256, seed=4, spacing=0.01, n_min=2000, n_max=2000
         }
         out.append((cfg, scen))
     return out
+
+
+def diff_block(nx=46, ny=46, nz=47, spacing=0.01, seed=5, v_std=0.1, fixed_iters=None):
+    """Differentiable DFSPH scene: a block of nx*ny*nz fluid particles (46 x 46 x 47
+    = 99,452 by default) in the x/z-min corner of a tank 1.6 x 1.5 x 1.6 block
+    lengths with 3 boundary layers, dt = 5e-4 (``solver_cs`` 20; the CFL limit
+    binds only above 10 m/s), tolerances 1% / 0.1%.  ``fixed_iters`` = k makes
+    both solves run exactly k iterations (tolerances out of reach).  Returns
+    (config, scenario, initial-velocity function, target point): velocities are
+    seeded N(0, v_std) per component, the target is the block's centre plus a
+    seeded U(-0.05, 0.05) offset per axis."""
+    import numpy as np
+    Lx, Ly, Lz = nx * spacing, ny * spacing, nz * spacing
+    t = 3.5 * spacing
+    box_lo = [-t, -t, -t]
+    box_hi = [1.6 * Lx + t, 1.5 * Ly + t, 1.6 * Lz + t]
+    sp32 = float(np.float32(spacing))
+    shape = ((np.array(box_hi, np.float32) - np.array(box_lo, np.float32) + 1e-7) / sp32).astype(np.int32)
+    n_box = int(np.prod(shape.astype(np.int64)) - np.prod(np.maximum(shape.astype(np.int64) - 6, 0)))
+    if fixed_iters:
+        cfg = _config(cs=20, div_tol=1e9, comp_tol=1e9)
+        cfg["solver_iter_threshold_min"] = int(fixed_iters)
+    else:
+        cfg = _config(cs=20)
+    scen = {
+        "sim_env": {"global_part_size": spacing, "global_dynamic_viscosity": 0.01, "sim_dim": 3,
+                    "sim_space_lb": [b - 0.1 for b in box_lo],
+                    "sim_space_rt": [box_hi[0] + 0.1, box_hi[1] + 0.1, box_hi[2] + 0.1],
+                    "gravity": [0, -9.81, 0], "phase_num": 1, "phase_rest_density": [1000],
+                    "phase_color_hex": ["0x6F7DBC"]},
+        "fluid": {"max_part_num": nx * ny * nz, "objs": [_obj("cube", [0.0, 0.0, 0.0], [Lx, Ly, Lz], [1], [0, 0, 0])]},
+        "bound": {"max_part_num": n_box, "objs": [_obj("box", box_lo, box_hi, [1], [0, 0, 0], layers=3)]},
+    }
+    rng = np.random.default_rng(seed)
+    target = np.array([0.5 * Lx, 0.5 * Ly, 0.5 * Lz]) + rng.uniform(-0.05, 0.05, 3)
+
+    def velocities(n):
+        r = np.random.default_rng(seed + 1)
+        return (r.standard_normal((n, 3)) * v_std).astype(np.float32)
+    return cfg, scen, velocities, target
