@@ -348,7 +348,7 @@ def run_adjoint(reps, warmup, dev, substeps=64, checkpoint_every=8):
         if r >= warmup:
             fw.append(ev[0].elapsed_time(ev[1]))
             bw.append(ev[1].elapsed_time(ev[2]))
-        gnorm, gmu, loss = float(v.grad.norm()), float(mu.grad), float(L)
+        gnorm, gmu, loss = float(v.grad.norm()), float(mu.grad), float(L.detach())
     st = roll.solver.stats()
     roll.close()
     fwm, bwm = sum(fw) / len(fw), sum(bw) / len(bw)

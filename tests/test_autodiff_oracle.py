@@ -13,11 +13,11 @@ from oracle import sph_autodiff as A
 from oracle import sph_oracle as O
 
 
-def small_scene(nx=6, ny=6, nz=6, fixed_iters=2):
+def small_scene(nx=6, ny=6, nz=6, fixed_iters=2, relax=1.0):
     """The differentiable workload at a small size, as (params, numpy sets, autodiff scene, x0, v0, target)."""
     from tichi_sph_gb300 import sph_config, workloads
     from tichi_sph_gb300.simulation import Simulation
-    c, s, vel, target = workloads.diff_block(nx=nx, ny=ny, nz=nz, fixed_iters=fixed_iters)
+    c, s, vel, target = workloads.diff_block(nx=nx, ny=ny, nz=nz, fixed_iters=fixed_iters, relax=relax)
     cfg = sph_config.Config(c, s)
     sim = Simulation(cfg, device="cpu")
     sim.init_scenario()

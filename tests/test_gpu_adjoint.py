@@ -1,11 +1,19 @@
 """The hand-written CUDA adjoint against the FP64 oracle (needs a GPU).
 
-Workload: the differentiable dam-block scene at 2,028 particles (13 x 12 x 13)
-in its tank, 16 substeps at dt = 5e-4 with both solves fixed at two iterations,
+Workload: the differentiable block scene at 2,028 particles (13 x 12 x 13) in
+its tank, emitted 3% denser than rest spacing, 16 substeps at dt = 5e-4 with
+both solves fixed at two iterations,
 loss = |centre of mass - target|^2 + 0.1 mean(((rho - rho0) / rho0)^2),
 gradients with respect to the initial velocity field and the viscosity.  The
 reference values are FP64: torch.autograd through the autodiff oracle and
 central finite differences of the oracle's forward.  Bar: 1e-3 relative.
+
+Why compressed: psi_adv = max(s, 0) puts a kink in the step wherever s = 0,
+and in a block at exactly rest spacing many particles sit at s ~ 0, where the
+FP32 and FP64 forwards take different branches: the oracle's own gradient run
+in FP32 then differs from its FP64 gradient by ~5e-3.  At 3% compression the
+interior is robustly active (the FP32 oracle differs by ~2e-4), so the check
+measures the adjoint rather than the branch choice.
 """
 import numpy as np
 import pytest
@@ -22,13 +30,13 @@ def _need_cuda():
 STEPS = 16
 
 
-def _setup(steps=STEPS, K=8, nx=13, ny=12, nz=13, fixed_iters=2):
+def _setup(steps=STEPS, K=8, nx=13, ny=12, nz=13, fixed_iters=2, relax=0.97):
     from oracle import sph_autodiff as A
     from oracle import sph_oracle as O
     from tichi_sph_gb300 import sph_config, workloads
     from tichi_sph_gb300.adjoint import DiffRollout
     from tichi_sph_gb300.simulation import Simulation
-    c, s, vel, target = workloads.diff_block(nx=nx, ny=ny, nz=nz, fixed_iters=fixed_iters)
+    c, s, vel, target = workloads.diff_block(nx=nx, ny=ny, nz=nz, fixed_iters=fixed_iters, relax=relax)
     cfg = sph_config.Config(c, s)
     sim = Simulation(cfg, device="cuda")
     sim.init_scenario()
@@ -53,7 +61,7 @@ def _cuda_grad(sim, roll, v0, target, mu=0.01):
     L = com_density_loss(x.double(), rho.double(), sim.fluid.mass[:n].double(), sim.fluid.rest_density[:n].double(),
                          torch.as_tensor(target, device="cuda"))
     L.backward()
-    return float(L), v.grad.detach().cpu().double(), float(m.grad), x.detach().cpu().double()
+    return float(L.detach()), v.grad.detach().cpu().double(), float(m.grad), x.detach().cpu().double()
 
 
 def _ref_loss(sc, x0, v0, mu, target, steps=STEPS):
@@ -110,7 +118,7 @@ def test_adjoint_with_convergence_tolerances():
     """Solver loops on their tolerances (the workload's own 1% / 0.1%): the
     recorded iteration counts drive the reverse sweeps; the gradients are finite."""
     _need_cuda()
-    sim, roll, v0, target, sc, x0, p = _setup(fixed_iters=None, steps=8)
+    sim, roll, v0, target, sc, x0, p = _setup(fixed_iters=None, steps=8, relax=1.0)
     L, gv, gmu, xT = _cuda_grad(sim, roll, v0, target)
     roll.close()
     assert np.isfinite(L) and torch.isfinite(gv).all() and np.isfinite(gmu)

@@ -136,13 +136,14 @@ def batched_dambreaks(n_scenes=256, seed=4, spacing=0.01, n_min=2000, n_max=2000
     return out
 
 
-def diff_block(nx=46, ny=46, nz=47, spacing=0.01, seed=5, v_std=0.1, fixed_iters=None):
+def diff_block(nx=46, ny=46, nz=47, spacing=0.01, seed=5, v_std=0.1, fixed_iters=None, relax=1.0):
     """Differentiable DFSPH scene: a block of nx*ny*nz fluid particles (46 x 46 x 47
     = 99,452 by default) in the x/z-min corner of a tank 1.6 x 1.5 x 1.6 block
     lengths with 3 boundary layers, dt = 5e-4 (``solver_cs`` 20; the CFL limit
     binds only above 10 m/s), tolerances 1% / 0.1%.  ``fixed_iters`` = k makes
     both solves run exactly k iterations (tolerances out of reach).  Returns
-    (config, scenario, initial-velocity function, target point): velocities are
+    (config, scenario, initial-velocity function, target point); ``relax`` < 1
+    emits the same lattice at relax x spacing (a compressed block).  Velocities are
     seeded N(0, v_std) per component, the target is the block's centre plus a
     seeded U(-0.05, 0.05) offset per axis."""
     import numpy as np
@@ -164,7 +165,8 @@ def diff_block(nx=46, ny=46, nz=47, spacing=0.01, seed=5, v_std=0.1, fixed_iters
                     "sim_space_rt": [box_hi[0] + 0.1, box_hi[1] + 0.1, box_hi[2] + 0.1],
                     "gravity": [0, -9.81, 0], "phase_num": 1, "phase_rest_density": [1000],
                     "phase_color_hex": ["0x6F7DBC"]},
-        "fluid": {"max_part_num": nx * ny * nz, "objs": [_obj("cube", [0.0, 0.0, 0.0], [Lx, Ly, Lz], [1], [0, 0, 0])]},
+        "fluid": {"max_part_num": nx * ny * nz, "objs": [
+            _obj("cube", [0.0, 0.0, 0.0], [Lx * relax, Ly * relax, Lz * relax], [1], [0, 0, 0], rf=relax)]},
         "bound": {"max_part_num": n_box, "objs": [_obj("box", box_lo, box_hi, [1], [0, 0, 0], layers=3)]},
     }
     rng = np.random.default_rng(seed)
