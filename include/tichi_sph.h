@@ -70,6 +70,8 @@ typedef struct tsph_params {
     float surface_tension_gamma;
     int32_t fbm_enabled;    /* run the volume-fraction block, main.py:244-250 */
     int32_t fbm_max_passes; /* cap on its pass loop (the reference has none) */
+    int32_t wc_gamma;       /* solver_wc_gamma (integer field, sph_config.py:167) */
+    int32_t wcsph_enabled;  /* run the weakly compressible pressure block, main.py:238-242 */
 } tsph_params;
 
 /* Views of one particle set: the fields of `Fluid`, sph_obj.py:24-63, in the
@@ -84,6 +86,7 @@ typedef struct tsph_set {
     float *W, *sph_density, *sph_compression, *psi_adv;
     float *alpha, *alpha_1, *alpha_2;
     float *normal, *drift_vel, *fbm_zeta;
+    float *pressure;        /* written by the weakly compressible block (fluid) */
     int32_t *flag;
     int32_t *neighb_cell_seq, *neighb_in_cell_seq, *neighb_cell_structured_seq;
 } tsph_set;
@@ -215,6 +218,17 @@ int tsph_fluid_density_noalloc(const tsph_params *params, const float *fluid_pos
                                const float *fluid_rest_volume, int64_t n_fluid, const float *bound_pos,
                                const float *bound_mass, const float *bound_rest_volume, int64_t n_bound,
                                float *W, float *sph_density, float *sph_compression, void *stream);
+
+/* Particle-to-grid velocity map, map_velocity (sph.py:382-397; called at the
+ * end of sph_step, main.py:254): for every node I of a regular grid with
+ * positions lb + I * dist (shape[0..dim-1], C order) writes
+ * grid_vel[I] = sum_j X_j / psi_j * vel_j * W(|pos_I - pos_j|) over the fluid
+ * particles of the template cells around the node's cell.  As in the
+ * reference the candidates come from the cell grid of the last step (built at
+ * its start) and positions / velocities / X / psi are the set's current
+ * values.  Call after a step; grid_vel is [prod(shape)][dim] device FP32. */
+int tsph_map_velocity(tsph_ctx *ctx, const tsph_set *fluid, const float *lb, float dist, const int32_t *shape,
+                      float *grid_vel, void *stream);
 
 /* ---------------------------------------------------------------- adjoint
  * Hand-written reverse mode of the substep (no counterpart in the reference,

@@ -51,7 +51,7 @@ class HostSet:
             "mass": z(n), "rest_density": z(n), "rest_volume": z(n), "volume_frac": z(n, P),
             "volume_frac_tmp": z(n, P), "W": z(n), "sph_density": z(n), "sph_compression": z(n),
             "psi_adv": z(n), "alpha": z(n), "alpha_1": z(n, dim), "alpha_2": z(n), "normal": z(n, dim),
-            "drift_vel": z(n, P, dim), "fbm_zeta": z(n),
+            "drift_vel": z(n, P, dim), "fbm_zeta": z(n), "pressure": z(n),
             "flag": np.zeros(n, np.int32), "neighb_cell_seq": np.zeros(n, np.int32),
             "neighb_in_cell_seq": np.zeros(n, np.int32), "neighb_cell_structured_seq": np.zeros((n, dim), np.int32),
         }

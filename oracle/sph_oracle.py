@@ -64,6 +64,7 @@ class Params:
         p.iter_min = int(cfg["solver_iter_threshold_min"])
         p.iter_max = int(cfg["solver_iter_threshold_max"])
         p.cs = int(cfg["solver_cs"])
+        p.wc_gamma = int(cfg["solver_wc_gamma"])
         p.cfl_factor = rnd(cfg["solver_cfl_factor"])
         p.fbm_diffusion = rnd(cfg["solver_fbm_diffusion_term"])
         p.fbm_convection = rnd(cfg["solver_fbm_convection_term"])
@@ -216,10 +217,15 @@ class Grid:
 
     def pairs(self, obj, nobj):
         """Every (i, j) the reference's template loop visits (``sph.py:52-60``)."""
+        i, j = self.candidates(obj.neighb_cell_structured_seq, nobj)
+        return Pairs(i, j, obj.pos[i] - nobj.pos[j])
+
+    def candidates(self, base, nobj):
+        """(i, j): members j of nobj in the template cells around cell base[i]."""
         p = self.p
         ids, codes = self.members[nobj.uid]
         I, J = [], []
-        base = obj.neighb_cell_structured_seq
+        n = len(base)
         for t in p.template:
             q = dim_encode(base + t, p)
             ok = (q > 0) & (q < p.node_num)
@@ -229,17 +235,14 @@ class Grid:
             tot = int(cnt.sum())
             if tot == 0:
                 continue
-            ii = np.repeat(np.arange(obj.n), cnt)
+            ii = np.repeat(np.arange(n), cnt)
             start = np.repeat(lo, cnt)
             off = np.arange(tot) - np.repeat(np.cumsum(cnt) - cnt, cnt)
             I.append(ii)
             J.append(ids[start + off])
         if I:
-            i = np.concatenate(I)
-            j = np.concatenate(J)
-        else:
-            i = j = np.zeros(0, dtype=np.int64)
-        return Pairs(i, j, obj.pos[i] - nobj.pos[j])
+            return np.concatenate(I), np.concatenate(J)
+        return np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int64)
 
 
 def _sum(idx, vals, n):
@@ -370,6 +373,36 @@ def IPPE_update_vel_adv(pr, obj, nobj, p, dt):
     obj.vel_adv += _sum(i, (-(1 / dt) * coef / obj.mass[i])[:, None] * g[m], obj.n)
 
 
+def WC_pressure_val(obj, p):
+    """``sph.py:169-176``: p = rho0 cs^2 / gamma ((rho / rho0)^7 - 1), clamped at 0."""
+    pr = (obj.rest_density * p.cs ** 2 / p.wc_gamma) * ((obj.sph_density / obj.rest_density) ** 7 - 1)
+    obj.pressure[:] = np.maximum(pr, 0.0)
+
+
+def WC_pressure_acce(pr, obj, nobj, p):
+    """``sph.py:179-193``: acce_adv -= (p_i / rho_i^2 + p_j / rho_j^2) m_j W'(r) x_ij / r."""
+    m = pr.r > 0
+    i, j, x, r = pr.i[m], pr.j[m], pr.xij[m], pr.r[m]
+    pt = obj.pressure[i] / obj.sph_density[i] ** 2 + nobj.pressure[j] / nobj.sph_density[j] ** 2
+    obj.acce_adv += _sum(i, (-pt * nobj.mass[j] * W_grad(r, p) / r)[:, None] * x, obj.n)
+
+
+def map_velocity(grid, gpos, nobj, p):
+    """``sph.py:382-397``: velocity at grid nodes gpos [G, dim] from the template
+    cells of the cell grid built at the step's start and nobj's current state."""
+    i, j = grid.candidates(node_encode(gpos, p), nobj)
+    x = gpos[i] - nobj.pos[j]
+    r = np.sqrt(np.einsum("ij,ij->i", x, x))
+    w = nobj.X[j] / nobj.sph_psi[j] * W(r, p)
+    return _sum(i, w[:, None] * nobj.vel[j], len(gpos))
+
+
+def grid_positions(lb, dist, shape):
+    """Node positions of ``Grid`` (``sph_obj.py:341-344``), C order."""
+    idx = np.stack(np.meshgrid(*[np.arange(n) for n in shape], indexing="ij"), -1).reshape(-1, len(shape))
+    return np.asarray(lb, dtype=np.float64) + idx * float(dist)
+
+
 def SPH_advection_update_vel_adv(obj, dt):
     """``sph.py:247-250``."""
     obj.vel_adv[:] = obj.vel + obj.acce_adv * dt
@@ -470,8 +503,11 @@ def _solve(pff, pfb, fluid, bound, p, dt, tol):
     return it
 
 
-def sph_step(fluid, bound, p, dt, fbm=False, max_fbm_passes=None):
-    """``main.py:175-256`` (FBM block ``main.py:244-250`` when ``fbm``)."""
+def sph_step(fluid, bound, p, dt, fbm=False, max_fbm_passes=None, wc=False, map_grid=None):
+    """``main.py:175-256`` (FBM block ``main.py:244-250`` when ``fbm``; the weakly
+    compressible pressure block ``main.py:238-242`` when ``wc``; the particle-to-grid
+    map ``main.py:254`` when ``map_grid`` = dict(lb, dist, shape), result in
+    ``map_grid["vel"]``)."""
     grid = Grid(p, [fluid, bound])
     pff = grid.pairs(fluid, fluid)
     pfb = grid.pairs(fluid, bound)
@@ -497,6 +533,11 @@ def sph_step(fluid, bound, p, dt, fbm=False, max_fbm_passes=None):
     SPH_advection_surface_tension_acc(pff, fluid, fluid, p)
     SPH_advection_update_vel_adv(fluid, dt)
     k_inc = _solve(pff, pfb, fluid, bound, p, dt, p.compression_threshold)
+    if wc:
+        WC_pressure_val(fluid, p)
+        WC_pressure_acce(pff, fluid, fluid, p)
+        WC_pressure_acce(pfb, fluid, bound, p)
+        SPH_advection_update_vel_adv(fluid, dt)
     passes = 0
     if fbm:
         while fluid.general_flag > 0:
@@ -511,15 +552,19 @@ def sph_step(fluid, bound, p, dt, fbm=False, max_fbm_passes=None):
     SPH_update_mass(fluid, p)
     SPH_update_pos(fluid, dt)
     SPH_update_energy(fluid, p)
+    if map_grid is not None:
+        gpos = grid_positions(map_grid["lb"], map_grid["dist"], map_grid["shape"])
+        map_grid["vel"] = map_velocity(grid, gpos, fluid, p).reshape(tuple(map_grid["shape"]) + (p.dim,))
     return k_div, k_inc, passes
 
 
-def run_substep(fluid, bound, p, stats, fbm=False):
+def run_substep(fluid, bound, p, stats, fbm=False, wc=False, map_grid=None):
     """One substep of ``run_step`` (``main.py:347-352``): CFL, clock, step."""
     dt = cfl_condition(fluid, p)
     stats.dt = dt
     stats.time_count += dt
-    stats.div_iter, stats.incom_iter, stats.fbm_passes = sph_step(fluid, bound, p, dt, fbm=fbm)
+    stats.div_iter, stats.incom_iter, stats.fbm_passes = sph_step(fluid, bound, p, dt, fbm=fbm, wc=wc,
+                                                                  map_grid=map_grid)
     return stats
 
 

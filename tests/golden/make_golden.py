@@ -10,7 +10,12 @@ pure-Python Taichi stand-in in ``tests/golden/taichi_shim`` and every kernel bod
 The reference's ``main.py`` cannot be imported (it opens a GGUI window at import,
 ``main.py:383-415``), so ``_substep`` below replays its per-substep sequence:
 ``run_step`` (``main.py:339-352``) and ``sph_step`` (``main.py:175-256``), with the
-volume-fraction (FBM) block ``main.py:244-250`` enabled for VFSPH scenes.
+volume-fraction (FBM) block ``main.py:244-250`` enabled for VFSPH scenes, and --
+for the ``wcsph*`` scenes -- the weakly compressible pressure block
+``main.py:238-242`` and the particle-to-grid map ``main.py:254`` (both shipped
+commented out) enabled; ``map_velocity`` runs on a ``Grid`` whose shape is
+ceil((rt - lb) / dist) per axis, the intent of ``sph_obj.py:326`` (whose
+expression divides only ``lb``).
 
 For each scene in ``tests/golden/scenes`` two child processes run:
 
@@ -35,8 +40,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.environ.get("TICHI_REFERENCE", "/root/reference")
 SCENES = os.path.join(HERE, "scenes")
-STEPS = {"dfsph2d": 3, "dfsph2d_r2": 2, "dfsph3d": 2, "vfsph2d": 3, "vfsph3d": 2, "edge2d": 2}
+STEPS = {"dfsph2d": 3, "dfsph2d_r2": 2, "dfsph3d": 2, "vfsph2d": 3, "vfsph3d": 2, "edge2d": 2,
+         "wcsph2d": 3, "wcsph3d": 2}
 FBM_SCENES = {"vfsph2d", "vfsph3d"}
+WC_SCENES = {"wcsph2d", "wcsph3d"}
 VF_NOISE_SEED = 3
 
 PARTICLE_FIELDS = [
@@ -109,10 +116,16 @@ def _child(scene, mode):
 
     gv = R.GlobalVariable()
     fbm = scene in FBM_SCENES
+    wc = scene in WC_SCENES
+    grid = _Grid(R, config) if wc else None
     rec = {}
+    if grid is not None:
+        rec["grid_lb"], rec["grid_dist"], rec["grid_shape"] = grid.lb, grid.dist, np.array(grid.shape)
     for step in range(STEPS[scene]):
-        _substep(R, config, ngrid, fluid, bound, gv, fbm)
+        _substep(R, config, ngrid, fluid, bound, gv, fbm, wc, grid)
         p = "s%d_" % step
+        if grid is not None:
+            rec[p + "grid_vel"] = grid.vel.to_numpy()
         rec[p + "dt"] = config.dt[None]
         rec[p + "time_count"] = gv.time_count
         rec[p + "div_iter"] = gv.div_iter_count
@@ -131,7 +144,22 @@ def _child(scene, mode):
     np.savez_compressed(os.path.join(HERE, scene + ".steps.npz"), **rec)
 
 
-def _substep(R, config, ngrid, fluid, bound, gv, fbm):
+class _Grid:
+    """``Grid`` (sph_obj.py:326-344) with the shape ceil((rt - lb) / dist)."""
+
+    def __init__(self, R, config):
+        dim = config.dim[None]
+        self.lb = config.sim_space_lb[None].to_numpy().astype(np.float64)
+        rt = config.sim_space_rt[None].to_numpy().astype(np.float64)
+        self.dist = float(config.part_size[1] * config.neighb_grid_size_TO_global_part_size[None])
+        self.shape = tuple(int(x) for x in np.ceil((rt - self.lb) / self.dist))
+        self.vel = R.ti.Vector.field(dim, float, shape=self.shape)
+        self.pos = R.ti.Vector.field(dim, float, shape=self.shape)
+        idx = np.stack(np.meshgrid(*[np.arange(n) for n in self.shape], indexing="ij"), -1)
+        self.pos.from_numpy(self.lb + idx * self.dist)   # init_pos, sph_obj.py:341-344
+
+
+def _substep(R, config, ngrid, fluid, bound, gv, fbm, wc=False, grid=None):
     """run_step's substep body (main.py:347-352) around sph_step (main.py:175-256)."""
     R.cfl_condition(fluid)
     gv.time_count += config.dt[None]
@@ -184,6 +212,11 @@ def _substep(R, config, ngrid, fluid, bound, gv, fbm):
         gv.incom_iter_count += 1
         if gv.incom_iter_count > config.iter_threshold_max[None]:
             break
+    if wc:  # main.py:238-242, enabled
+        R.WC_pressure_val(fluid)
+        R.WC_pressure_acce(ngrid, fluid, fluid)
+        R.WC_pressure_acce(ngrid, fluid, bound)
+        R.SPH_advection_update_vel_adv(fluid)
     if fbm:  # main.py:244-250, enabled
         while fluid.general_flag[None] > 0:
             R.SPH_FBM_clean_tmp(fluid)
@@ -194,6 +227,8 @@ def _substep(R, config, ngrid, fluid, bound, gv, fbm):
     R.SPH_update_mass(fluid)
     R.SPH_update_pos(fluid)
     R.SPH_update_energy(fluid)
+    if grid is not None:  # main.py:254, enabled
+        R.map_velocity(ngrid, grid, fluid)
     gv.frame_div_iter += gv.div_iter_count
     gv.frame_incom_iter += gv.incom_iter_count
 

@@ -16,7 +16,9 @@ iteration counts exactly equal.  With the volume-fraction update on,
 two velocities, so it and the quantities built from it (``acce``, ``drift_vel``)
 are scaled by the velocity they were differenced from (max|v_adv| / dt, and
 max|v_adv| for ``drift_vel`` which carries a factor dt); ``volume_frac_tmp`` is an
-increment of ``volume_frac`` and is scaled by it.
+increment of ``volume_frac`` and is scaled by it.  With the weakly compressible
+block on (``wcsph*`` scenes) the fluid's ``pressure`` is compared too, and the
+particle-to-grid map's node velocities (1e-5 of their largest magnitude).
 """
 import numpy as np
 import pytest
@@ -31,7 +33,7 @@ TOL_ONE_STEP = {
     "pos": 2e-6, "vel": 1e-5, "vel_adv": 1e-5, "acce_adv": 1e-5, "mass": 2e-6, "rest_density": 2e-6,
     "volume_frac": 1e-5, "volume_frac_tmp": 1e-5, "W": 1e-5, "sph_density": 1e-5,
     "sph_compression": 1e-5, "psi_adv": 1e-5, "alpha": 1e-5, "alpha_1": 1e-5, "alpha_2": 1e-5,
-    "normal": 1e-5, "drift_vel": 1e-5, "fbm_zeta": 1e-5, "acce": 1e-5,
+    "normal": 1e-5, "drift_vel": 1e-5, "fbm_zeta": 1e-5, "acce": 1e-5, "pressure": 1e-5,
 }
 EXACT = ("neighb_cell_seq", "neighb_cell_structured_seq", "flag")
 BOUND_FIELDS = ("W", "sph_density", "sph_compression", "alpha_2", "alpha", "neighb_cell_seq",
@@ -56,8 +58,28 @@ def make_gpu(scene, fluid_arrays, bound_arrays, use_graph=True):
             getattr(o, k)[:n] = torch.as_tensor(np.asarray(v, dtype=np.float32), device="cuda").reshape(
                 getattr(o, k)[:n].shape)
         objs.append(o)
-    s = Solver(cfg, objs[0], objs[1], fbm=scene in G.FBM_SCENES, use_graph=use_graph)
+    s = Solver(cfg, objs[0], objs[1], fbm=scene in G.FBM_SCENES, use_graph=use_graph,
+               wcsph=scene in G.WC_SCENES)
     return cfg, objs[0], objs[1], s
+
+
+def _substep_oracle(scene, ofl, obd, p, st, gold):
+    """One oracle substep with the scene's optional blocks; returns the
+    particle-to-grid map's node velocities for WC scenes (else None)."""
+    wc = scene in G.WC_SCENES
+    mg = G.map_grid(gold) if wc else None
+    O.run_substep(ofl, obd, p, st, fbm=scene in G.FBM_SCENES, wc=wc, map_grid=mg)
+    return mg["vel"] if wc else None
+
+
+def _check_map(scene, tag, cfg, solver, ref):
+    from tichi_sph_gb300.sph_obj import Grid
+    grid = Grid(cfg, device="cuda")
+    solver.map_velocity(grid)
+    a = grid.vel.cpu().numpy().astype(np.float64)
+    assert a.shape == ref.shape, (scene, a.shape, ref.shape)
+    err = float(np.abs(a - ref).max()) / max(float(np.abs(ref).max()), 1e-30)
+    assert err <= 1e-5, "%s %s grid velocity rel err %.3g" % (scene, tag, err)
 
 
 def make_oracle(scene, fluid_arrays, bound_arrays):
@@ -101,6 +123,8 @@ def _fluid_fields(scene, p):
         fields.append("normal")
     if scene in G.FBM_SCENES:
         fields += ["volume_frac", "volume_frac_tmp", "drift_vel", "fbm_zeta", "acce"]
+    if scene in G.WC_SCENES:
+        fields.append("pressure")
     return fields
 
 
@@ -127,7 +151,9 @@ def test_one_step_from_reference_states(scene, use_graph):
         st.time_count = t0
         solver.substep()
         gs = solver.stats()
-        O.run_substep(ofl, obd, p, st, fbm=scene in G.FBM_SCENES)
+        gref = _substep_oracle(scene, ofl, obd, p, st, gold)
+        if gref is not None:
+            _check_map(scene, "step%d" % step, cfg, solver, gref)
         assert gs["div_iter"] == st.div_iter and gs["incom_iter"] == st.incom_iter, (scene, step, gs, vars(st))
         assert gs["dt"] == pytest.approx(st.dt, rel=1e-6)
         if scene in G.FBM_SCENES:
@@ -156,7 +182,7 @@ def test_trajectory_against_oracle(scene):
     for step in range(G.n_steps(gold)):
         solver.substep()
         gs = solver.stats()
-        O.run_substep(ofl, obd, p, st, fbm=scene in G.FBM_SCENES)
+        _substep_oracle(scene, ofl, obd, p, st, gold)
         assert gs["div_iter"] == st.div_iter and gs["incom_iter"] == st.incom_iter
         assert gs["time_count"] == pytest.approx(st.time_count, rel=1e-6)
         dens = float(np.abs(ofl.sph_density).max(initial=0.0))

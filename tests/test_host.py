@@ -126,3 +126,20 @@ def test_struct_layouts_match_header():
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
     assert [int(x) for x in out] == [ctypes.sizeof(_native.Params), ctypes.sizeof(_native.Set),
                                     ctypes.sizeof(_native.Stats)]
+
+
+def test_map_grid_shape_matches_reference_run():
+    """The particle-to-grid Grid (ceil((rt - lb) / dist) per axis) has the shape
+    and node positions the golden runs used."""
+    from tichi_sph_gb300 import sph_config
+    from tichi_sph_gb300.sph_obj import Grid
+    from tests import golden_io as G
+    for scene in sorted(G.WC_SCENES):
+        cfg = sph_config.load(*G.paths(scene))
+        _, gold = G.load(scene)
+        g = Grid(cfg, device="cpu")
+        assert g.shape == tuple(int(x) for x in gold["grid_shape"])
+        ref = G.map_grid(gold)
+        assert abs(g.dist - ref["dist"]) <= 1e-7 * ref["dist"]
+        import numpy as np
+        np.testing.assert_allclose(g.pos[(0,) * len(g.shape)].numpy(), ref["lb"], rtol=0, atol=1e-7)

@@ -20,9 +20,14 @@ def test_oracle_matches_reference_run(scene):
     init, gold = G.load(scene)
     fl, bd = O.sets_from_arrays(p, G.init_arrays(init, "fluid"), G.init_arrays(init, "bound"))
     st = O.Stats()
+    wc = scene in G.WC_SCENES
     for s in range(G.n_steps(gold)):
-        O.run_substep(fl, bd, p, st, fbm=scene in G.FBM_SCENES)
+        mg = G.map_grid(gold) if wc else None
+        O.run_substep(fl, bd, p, st, fbm=scene in G.FBM_SCENES, wc=wc, map_grid=mg)
         pre = "s%d_" % s
+        if wc:
+            g = gold[pre + "grid_vel"]
+            assert float(np.abs(mg["vel"] - g).max()) <= RTOL * max(float(np.abs(g).max()), 1e-12), (scene, s)
         assert st.div_iter == int(gold[pre + "div_iter"])
         assert st.incom_iter == int(gold[pre + "incom_iter"])
         assert st.dt == pytest.approx(float(gold[pre + "dt"]), rel=1e-14)
@@ -36,7 +41,7 @@ def test_oracle_matches_reference_run(scene):
             assert abs(val - g) <= RTOL * max(abs(g), floor), key
         for name, obj in (("fluid", fl), ("bound", bd)):
             dens_scale = float(np.abs(gold[pre + name + "_sph_density"]).max(initial=0.0))
-            for f in G.COMPARED:
+            for f in G.COMPARED + (G.WC_COMPARED if wc and name == "fluid" else []):
                 a = np.asarray(getattr(obj, f), dtype=np.float64)
                 b = gold[pre + name + "_" + f].astype(np.float64)
                 if f in ("flag", "neighb_cell_seq", "neighb_cell_structured_seq"):

@@ -13,8 +13,8 @@ there is no CPU or Python fallback.
 """
 from . import sph_config  # noqa: F401
 from .sph_config import Config, load, from_argv  # noqa: F401
-from .sph_obj import Fluid, Ngrid, GlobalVariable  # noqa: F401
-from .sph import Solver, cfl_condition, sph_step  # noqa: F401
+from .sph_obj import Fluid, Grid, Ngrid, GlobalVariable  # noqa: F401
+from .sph import Solver, cfl_condition, map_velocity, sph_step  # noqa: F401
 from .simulation import Simulation  # noqa: F401
 
 __version__ = "0.1.0"

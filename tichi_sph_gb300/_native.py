@@ -32,13 +32,13 @@ class Params(C.Structure):
         ("divergence_threshold", _f), ("compression_threshold", _f),
         ("iter_min", _i32), ("iter_max", _i32), ("cs", _i32), ("cfl_factor", _f),
         ("fbm_diffusion", _f), ("fbm_convection", _f), ("surface_tension_gamma", _f),
-        ("fbm_enabled", _i32), ("fbm_max_passes", _i32),
+        ("fbm_enabled", _i32), ("fbm_max_passes", _i32), ("wc_gamma", _i32), ("wcsph_enabled", _i32),
     ]
 
 
 SET_FLOAT_FIELDS = ["pos", "vel", "vel_adv", "acce", "acce_adv", "mass", "rest_density", "rest_volume",
                     "volume_frac", "volume_frac_tmp", "W", "sph_density", "sph_compression", "psi_adv",
-                    "alpha", "alpha_1", "alpha_2", "normal", "drift_vel", "fbm_zeta"]
+                    "alpha", "alpha_1", "alpha_2", "normal", "drift_vel", "fbm_zeta", "pressure"]
 SET_INT_FIELDS = ["flag", "neighb_cell_seq", "neighb_in_cell_seq", "neighb_cell_structured_seq"]
 
 
@@ -86,6 +86,7 @@ SIGNATURES = {
     "tsph_profile_phases": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_int, _fp, C.c_void_p]),
     "tsph_fluid_density_noalloc": (C.c_int, [C.POINTER(Params), _fp, _fp, _fp, _i64, _fp, _fp, _fp, _i64,
                                              _fp, _fp, _fp, C.c_void_p]),
+    "tsph_map_velocity": (C.c_int, [CtxP, C.POINTER(Set), _fp, C.c_float, _ip, _fp, C.c_void_p]),
     "tsph_tape_create": (C.c_int, [CtxP, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "tsph_tape_destroy": (C.c_int, [C.c_void_p]),
     "tsph_substep_record": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p, C.c_int, C.c_void_p]),

@@ -168,6 +168,7 @@ int enqueue_step(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t
     if (c.rec_tape) launch_tape_vmid(c, st);
     rc = solve(c, kSolveDens, st, graph);
     if (rc) return rc;
+    if (c.p.wcsph_enabled) launch_wc(c, b, st);
     if (c.p.fbm_enabled) {
         rc = fbm_loop(c, st, graph);
         if (rc) return rc;
@@ -301,6 +302,7 @@ void make_scene(const tsph_params &p, SceneConst &c) {
     c.iter_min = p.iter_min;
     c.iter_max = p.iter_max;
     c.fbm_max_passes = p.fbm_max_passes > 0 ? p.fbm_max_passes : 1000;
+    c.wc_gamma = p.wc_gamma;
     c.div_tol = p.divergence_threshold;
     c.comp_tol = p.compression_threshold;
 }
@@ -312,6 +314,7 @@ int check_params(const tsph_params &p) {
     if (!(p.kernel_h > 0.f)) return fail(TSPH_ERR_INVALID, "kernel_h must be positive");
     if (p.node_num < 1 || p.node_num > 0x7ffffff0ll) return fail(TSPH_ERR_INVALID, "node_num out of range");
     if (p.cs == 0) return fail(TSPH_ERR_INVALID, "solver_cs must be nonzero");
+    if (p.wcsph_enabled && p.wc_gamma == 0) return fail(TSPH_ERR_INVALID, "solver_wc_gamma must be nonzero");
     return TSPH_OK;
 }
 
@@ -328,9 +331,9 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
         if (rc) return rc;
         if (ps[s].dim != ps[0].dim || ps[s].phase_num != ps[0].phase_num ||
             ps[s].solver_type != ps[0].solver_type || ps[s].neighb_range != ps[0].neighb_range ||
-            ps[s].fbm_enabled != ps[0].fbm_enabled)
+            ps[s].fbm_enabled != ps[0].fbm_enabled || ps[s].wcsph_enabled != ps[0].wcsph_enabled)
             return fail(TSPH_ERR_INVALID, "scenes of a batch must share dim, phase_num, solver_type, "
-                                          "neighb_range and fbm_enabled");
+                                          "neighb_range, fbm_enabled and wcsph_enabled");
         if (batch && (fn[s] < 0 || bn[s] < 0)) return fail(TSPH_ERR_INVALID, "negative scene particle count");
     }
     if (!batch && (capf < 0 || capb < 0)) return fail(TSPH_ERR_INVALID, "negative capacity");
@@ -436,6 +439,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     F.flagpass = A.get<int>(fcap);
     F.nbr = A.get<int>((long long)k.nbr_max * fcap);
     F.nbr_cnt = A.get<unsigned int>(fcap);
+    F.wcp = ps[0].wcsph_enabled ? A.get<float2>(fcap) : nullptr;
     BoundBuf &B = c.B;
     B.cap = bcap;
     B.count = A.get<int>(nn);
@@ -452,6 +456,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     B.comp = A.get<float>(bcap);
     B.a2 = A.get<float>(bcap);
     B.alpha = A.get<float>(bcap);
+    B.wcp2 = ps[0].wcsph_enabled ? A.get<float>(bcap) : nullptr;
     c.S.partials_len = 2 * 8 * ((fcap + bcap) / kBlock) + 2 * ublk + 64;  // up to 8 threads per particle
     c.S.partials = A.get<double>(c.S.partials_len);
     const int64_t nscan = (nn + 4095) / 4096 + 1;

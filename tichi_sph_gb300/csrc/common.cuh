@@ -40,7 +40,7 @@ struct SceneConst {
     float mu, gamma, fbm_c, fbm_D;
     float rho_phase[kMaxP];
     float part_size, cfl;
-    int cs, iter_min, iter_max, fbm_max_passes;
+    int cs, iter_min, iter_max, fbm_max_passes, wc_gamma;
     float div_tol, comp_tol;
     // caller order [f_user, f_user + f_n); sorted slots [f_slot, f_slot + f_slots)
     long long f_user, f_n, f_slot, f_slots;
@@ -185,6 +185,7 @@ struct FluidBuf {
     // nbr_cnt[s] packs the two counts (fluid | boundary << 16) or is kNbrOverflow.
     int *nbr;
     unsigned int *nbr_cnt;
+    float2 *wcp;             // weakly compressible block: (pressure, pressure / rho^2)
 };
 
 struct BoundBuf {
@@ -195,6 +196,7 @@ struct BoundBuf {
     float4 *vadv;      // boundary vel_adv (never advanced by the reference)
     float *kappa;      // psi_adv / alpha of the boundary particle
     float *W, *rho, *comp, *a2, *alpha;
+    float *wcp2;       // pressure / rho^2 of the boundary particle (weakly compressible block)
 };
 
 struct Scratch {

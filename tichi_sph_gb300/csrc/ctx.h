@@ -49,6 +49,9 @@ void launch_psi(tsph_ctx &c, cudaStream_t st);
 void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
 void launch_advect(tsph_ctx &c, cudaStream_t st);
 
+// wcsph.cu
+void launch_wc(tsph_ctx &c, const tsph_set &b, cudaStream_t st);
+
 // adjoint.cu: recording hooks of the forward step
 void launch_tape_state(tsph_ctx &c, cudaStream_t st);
 void launch_tape_iter(tsph_ctx &c, int kind, cudaStream_t st);

@@ -373,6 +373,7 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
         U.sph_density[pid] = F.rho[s];
         U.sph_compression[pid] = F.comp[s];
         U.psi_adv[pid] = F.psiadv[s];
+        if (F.wcp && U.pressure) U.pressure[pid] = F.wcp[s].x;
         U.alpha[pid] = F.mpsi[s].w;
         U.alpha_2[pid] = F.a2[s];
         if (s - c.f_slot < st.f_in) {

@@ -14,7 +14,7 @@ import warnings
 import numpy as np
 
 from .sph import Solver
-from .sph_obj import Fluid, GlobalVariable, Ngrid
+from .sph_obj import Fluid, GlobalVariable, Grid, Ngrid
 
 
 def warn(*message):
@@ -67,7 +67,7 @@ def write_ply(path, frame_num, dim, num, pos):
 class Simulation:
     """The reference's module-level state of ``main.py`` as one object."""
 
-    def __init__(self, config, fbm=False, use_graph=True, device=None, out_dir=None):
+    def __init__(self, config, fbm=False, use_graph=True, device=None, out_dir=None, wcsph=False, map_grid=False):
         self.config = config
         self.ngrid = Ngrid(config)
         self.fluid = Fluid(config.fluid_max_part_num[None], config, uid=0, device=device)
@@ -76,14 +76,18 @@ class Simulation:
         self.scenario_wait_buffer = []
         self.inlets = []
         self.fbm = fbm
+        self.wcsph = wcsph
         self.use_graph = use_graph
+        # the particle-to-grid map the reference ships commented out (main.py:254)
+        self.grid = Grid(config, device=device) if map_grid else None
         self.out_dir = out_dir or config.solver_type
         self._solver = None
 
     @property
     def solver(self):
         if self._solver is None:
-            self._solver = Solver(self.config, self.fluid, self.bound, fbm=self.fbm, use_graph=self.use_graph)
+            self._solver = Solver(self.config, self.fluid, self.bound, fbm=self.fbm, use_graph=self.use_graph,
+                                  wcsph=self.wcsph)
         return self._solver
 
     # ---------------------------------------------------------------- scenario
@@ -184,6 +188,8 @@ class Simulation:
         self.refresh_scenario()
         s = self.solver
         s.substep()
+        if self.grid is not None:
+            s.map_velocity(self.grid)
         st = s.stats()
         gv = self.globalvar
         gv.time_count += st["dt"]

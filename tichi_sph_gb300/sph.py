@@ -20,11 +20,12 @@ class Solver:
     """One solver context for a (fluid, boundary) pair of particle sets.
 
     ``fbm`` enables the volume-fraction update block that the reference ships
-    commented out (``main.py:244-250``); ``use_graph=False`` runs the solver loops
+    commented out (``main.py:244-250``), ``wcsph`` its weakly compressible
+    pressure block (``main.py:238-242``); ``use_graph=False`` runs the solver loops
     host-driven, reading the convergence value every iteration as the reference
     does (``main.py:201,222``)."""
 
-    def __init__(self, config, fluid, bound, fbm=False, use_graph=True, fbm_max_passes=1000):
+    def __init__(self, config, fluid, bound, fbm=False, use_graph=True, fbm_max_passes=1000, wcsph=False):
         if fluid.device.type != "cuda" or bound.device.type != "cuda":
             raise RuntimeError("tichi_sph_gb300: particle sets must live on a CUDA device")
         self.config = config
@@ -34,7 +35,8 @@ class Solver:
         self.device = fluid.device
         L = _native.lib()
         self._lib = L
-        params = config.to_params(fbm_enabled=self.fbm, fbm_max_passes=fbm_max_passes)
+        self.wcsph = bool(wcsph)
+        params = config.to_params(fbm_enabled=self.fbm, fbm_max_passes=fbm_max_passes, wcsph_enabled=self.wcsph)
         ctx = _native.CtxP()
         with torch.cuda.device(self.device):
             check(L.tsph_create(_native.C.byref(params), fluid.max_part_num, bound.max_part_num,
@@ -131,6 +133,18 @@ class Solver:
                   "tsph_profile_phases")
         return dict(zip(_native.PHASES, [float(v) for v in out]))
 
+    def map_velocity(self, grid):
+        """``map_velocity(ngrid, grid, fluid)``, sph.py:382-397: fills ``grid.vel``
+        from the fluid's current state and the cell grid of the last step."""
+        C = _native.C
+        lb = (C.c_float * 3)(*[float(x) for x in grid.lb] + [0.0] * (3 - len(grid.lb)))
+        shape = (C.c_int32 * 3)(*[int(x) for x in grid.shape] + [1] * (3 - len(grid.shape)))
+        out = grid.vel
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_map_velocity(self.ctx, C.byref(self.fluid.native_set()), lb, float(grid.dist), shape,
+                                              C.cast(out.data_ptr(), C.POINTER(C.c_float)),
+                                              C.c_void_p(_stream_handle(self.device))), "tsph_map_velocity")
+
     def neighbor_stats(self):
         """Per-particle neighbour counts (fluid, boundary) and set hashes."""
         nf, nb = self.fluid.part_num[None], self.bound.part_num[None]
@@ -148,6 +162,11 @@ class Solver:
                 _native.C.cast(bc.data_ptr(), _native._ip), _native.C.cast(bh.data_ptr(), u64p),
                 _native.C.c_void_p(_stream_handle(dev))), "tsph_neighbor_stats")
         return fc[:nf], fh[:nf], bc[:nb], bh[:nb]
+
+
+def map_velocity(solver, grid):
+    """Module-level form of ``map_velocity(ngrid, grid, fluid)`` (sph.py:382-397)."""
+    solver.map_velocity(grid)
 
 
 def cfl_condition(solver):

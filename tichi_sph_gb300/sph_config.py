@@ -193,7 +193,7 @@ class Config:
         self.neighb_search_template = tmpl
 
     # -------------------------------------------------------------------- C ABI
-    def to_params(self, fbm_enabled=False, fbm_max_passes=1000):
+    def to_params(self, fbm_enabled=False, fbm_max_passes=1000, wcsph_enabled=False):
         """The :class:`_native.Params` struct handed to ``tsph_create``."""
         p = _native.Params()
         d = self.dim[None]
@@ -225,6 +225,8 @@ class Config:
         p.surface_tension_gamma = float(self.surface_tension_gamma[None])
         p.fbm_enabled = 1 if fbm_enabled else 0
         p.fbm_max_passes = int(fbm_max_passes)
+        p.wc_gamma = int(self.wc_gamma[None])
+        p.wcsph_enabled = 1 if wcsph_enabled else 0
         return p
 
 

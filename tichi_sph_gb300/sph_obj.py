@@ -216,6 +216,27 @@ class Ngrid:
         self.part_uid_in_node = None
 
 
+class Grid:
+    """Eulerian grid of the particle-to-grid map, ``sph_obj.py:326-344``: node
+    positions lb + I * dist with dist = part_size * neighb_grid_size ratio.
+    The shape is ceil((rt - lb) / dist) per axis -- what ``sph_obj.py:326``
+    means; its expression divides only ``lb`` (operator precedence).  ``vel``
+    and ``pos`` are [*shape, dim] tensors (C order)."""
+
+    def __init__(self, config, device=None):
+        d = config.dim[None]
+        self.dim = d
+        self.lb = np.array([float(x) for x in config.sim_space_lb[None]], dtype=np.float32)
+        rt = np.array([float(x) for x in config.sim_space_rt[None]], dtype=np.float32)
+        self.dist = float(np.float32(float(config.part_size[1]) * float(config.neighb_grid_size_TO_global_part_size[None])))
+        self.shape = tuple(int(x) for x in np.ceil((rt.astype(np.float64) - self.lb) / self.dist))
+        self.size = int(np.prod(self.shape))
+        self.device = torch.device(device) if device is not None else _default_device()
+        idx = np.stack(np.meshgrid(*[np.arange(n) for n in self.shape], indexing="ij"), -1)
+        self.pos = torch.as_tensor((self.lb + idx * np.float32(self.dist)).astype(np.float32), device=self.device)
+        self.vel = torch.zeros(self.shape + (d,), dtype=torch.float32, device=self.device)
+
+
 class GlobalVariable:
     """Host-side timers and counters, ``sph_obj.py:347-368`` (no window flags)."""
 
