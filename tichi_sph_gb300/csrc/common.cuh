@@ -218,6 +218,15 @@ __device__ __forceinline__ float kwg(float q) {
     float b = 1.f - q;
     return q <= 0.5f ? a : (q < 1.f ? -6.f * b * b : 0.f);
 }
+// r = |x| and 1 / r from r^2 with the hardware reciprocal square root (rsqrtf,
+// within a few ulp): cheaper than an IEEE square root plus an IEEE division
+// per pair.  r^2 = 0 gives r = 0 and 1 / r = 0.
+__device__ __forceinline__ float pair_rinv(float r2, float &r) {
+    const float inv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+    r = r2 * inv;
+    return inv;
+}
+
 __device__ __forceinline__ float kcoh(float q) {
     float b = 1.f - q;
     float t = b * b * b * q * q * q;

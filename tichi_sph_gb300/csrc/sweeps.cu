@@ -67,7 +67,8 @@ __device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf 
     const float r2 = dx * dx + dy * dy + dz * dz;
     if (r2 < g.h2) {
         const float2 mv = F.mv[j];
-        const float r = sqrtf(r2);
+        float r;
+        const float ri = pair_rinv(r2, r);
         const float q = r * g.inv_h;
         const float w = kw(q) * g.sig;
         wsum += w;
@@ -75,7 +76,7 @@ __device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf 
         comp += w * mv.y;
         if (r2 > 0.f) {
             const float wg = kwg(q) * g.sig_h;
-            const float f = pj.w * wg / r;
+            const float f = pj.w * wg * ri;
             a1x += f * dx;
             a1y += f * dy;
             a1z += f * dz;
@@ -92,14 +93,15 @@ __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf 
     const float r2 = dx * dx + dy * dy + dz * dz;
     if (r2 < g.h2) {
         const float2 mv = B.mv[j];
-        const float r = sqrtf(r2);
+        float r;
+        const float ri = pair_rinv(r2, r);
         const float q = r * g.inv_h;
         const float w = kw(q) * g.sig;
         wsum += w;
         rho += w * mv.x;
         comp += w * mv.y;
         if (r2 > 0.f) {
-            const float f = pj.w * kwg(q) * g.sig_h / r;
+            const float f = pj.w * kwg(q) * g.sig_h * ri;
             a1x += f * dx;
             a1y += f * dy;
             a1z += f * dz;
@@ -212,7 +214,9 @@ __global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, 
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (r2 < g.h2) {
                 const float2 mv = B.mv[j];
-                const float w = kw(sqrtf(r2) * g.inv_h) * g.sig;
+                float r;
+                pair_rinv(r2, r);
+                const float w = kw(r * g.inv_h) * g.sig;
                 wsum += w;
                 rho += w * mv.x;
                 comp += w * mv.y;
@@ -224,7 +228,9 @@ __global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, 
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (r2 < g.h2) {
                 const float2 mv = F.mv[j];
-                const float q = sqrtf(r2) * g.inv_h;
+                float r;
+                const float ri = pair_rinv(r2, r);
+                const float q = r * g.inv_h;
                 const float w = kw(q) * g.sig;
                 wsum += w;
                 rho += w * mv.x;
@@ -324,8 +330,9 @@ __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < g.h2 && r2 > 0.f) {
                     const float4 vj = vin[j];
-                    const float r = sqrtf(r2);
-                    const float f = kwg(r * g.inv_h) * g.sig_h / r * pj.w;
+                    float r;
+                    const float ri = pair_rinv(r2, r);
+                    const float f = kwg(r * g.inv_h) * g.sig_h * ri * pj.w;
                     acc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
                 }
             },
@@ -335,8 +342,9 @@ __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < g.h2 && r2 > 0.f) {
                     const float4 vj = B.vadv[j];
-                    const float r = sqrtf(r2);
-                    const float f = kwg(r * g.inv_h) * g.sig_h / r * pj.w;
+                    float r;
+                    const float ri = pair_rinv(r2, r);
+                    const float f = kwg(r * g.inv_h) * g.sig_h * ri * pj.w;
                     acc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
                 }
             });
@@ -403,8 +411,9 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
                     const float r2 = dx * dx + dy * dy + dz * dz;
                     if (r2 < g.h2 && r2 > 0.f) {
                         const float kj = F.kappa[j];
-                        const float r = sqrtf(r2);
-                        const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h / r);
+                        float r;
+                        const float ri = pair_rinv(r2, r);
+                        const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h * ri);
                         ax += f * dx;
                         ay += f * dy;
                         az += f * dz;
@@ -416,8 +425,9 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
                     const float r2 = dx * dx + dy * dy + dz * dz;
                     if (r2 < g.h2 && r2 > 0.f) {
                         const float kj = B.kappa[j];
-                        const float r = sqrtf(r2);
-                        const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h / r);
+                        float r;
+                        const float ri = pair_rinv(r2, r);
+                        const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h * ri);
                         ax += f * dx;
                         ay += f * dy;
                         az += f * dz;
@@ -483,8 +493,9 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < g.h2 && r2 > 0.f) {
-                    const float r = sqrtf(r2);
-                    const float f = -pj.w / F.mpsi[j].y * (kwg(r * g.inv_h) * g.sig_h) / r;
+                    float r;
+                    const float ri = pair_rinv(r2, r);
+                    const float f = -pj.w / F.mpsi[j].y * (kwg(r * g.inv_h) * g.sig_h) * ri;
                     nx += f * dx;
                     ny += f * dy;
                     nz += f * dz;
@@ -538,10 +549,11 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
             if (r2 < g.h2) {
                 const float4 vj = vin[j];
                 const float psij = F.mpsi[j].y;
-                const float r = sqrtf(r2);
+                float r;
+                const float ri = pair_rinv(r2, r);
                 const float wg = kwg(r * g.inv_h) * g.sig_h;
                 const float adx = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-                const float f = lap * (pj.w / psij) * wg / r * adx / (eps + r2);
+                const float f = lap * (pj.w / psij) * wg * ri * adx / (eps + r2);
                 vx += f * dx;
                 vy += f * dy;
                 vz += f * dz;
@@ -550,8 +562,9 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                 if (F.vf[j] > 0.99f) {
                     const float4 mpj = F.mpsi[j];
                     const float4 nj = F.normal[j];
-                    const float r = sqrtf(r2);
-                    const float coh = -gamma * mpj.x * (kcoh(r * g.inv_h) * c_coh) / r;
+                    float r;
+                    const float ri = pair_rinv(r2, r);
+                    const float coh = -gamma * mpj.x * (kcoh(r * g.inv_h) * c_coh) * ri;
                     const float fac = 2.f * mpi.z / (mpi.y + mpj.y);
                     sx += fac * (coh * dx + gamma * (ni.x - nj.x));
                     sy += fac * (coh * dy + gamma * (ni.y - nj.y));
