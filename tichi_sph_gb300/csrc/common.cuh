@@ -279,6 +279,30 @@ __device__ __forceinline__ void visit_candidates(const int *__restrict__ start, 
     }
 }
 
+// visit_candidates reading the scene's row geometry (nx, nx*ny, node_num,
+// cbase) from the scene table at every row instead of holding it in registers.
+template <int DIM, int TPP, class F>
+__device__ __forceinline__ void visit_candidates_lean(const int *__restrict__ start, const SceneConst *c, int R,
+                                                      long long code, long long shift, int q, F &&f) {
+    const int zr = (DIM == 3) ? R : 0;
+    for (int dz = -zr; dz <= zr; ++dz) {
+        for (int dy = -R; dy <= R; ++dy) {
+            const long long nx = *(volatile const long long *)&c->nx;
+            const long long nxny = *(volatile const long long *)&c->nxny;
+            const long long nn = *(volatile const long long *)&c->node_num;
+            const long long cb = *(volatile const long long *)&c->cbase;
+            const long long rc = code + dy * nx + dz * nxny;
+            long long lo = rc - R, hi = rc + R;
+            if (lo < 1) lo = 1;
+            if (hi > nn - 1) hi = nn - 1;
+            if (lo > hi) continue;
+            const int beg = (int)(__ldg(start + cb + lo) + shift);
+            const int end = (int)(__ldg(start + cb + hi + 1) + shift);
+            for (int j = beg + q; j < end; j += TPP) f(j);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------
 // Deterministic reductions in FP64 (warp shuffles, fixed trees).
 __device__ __forceinline__ double warp_sum(double v) {
@@ -426,15 +450,30 @@ __device__ __forceinline__ void for_each_neighbor_tpp(const SceneConst &c, const
     if (pc != kNbrOverflow) {
         const int nfl = (int)(pc & 0xffffu), nbo = (int)(pc >> 16);
         walk_blocks<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl, ff, fb);
-    } else {
-        // the grid geometry and the scan shifts are loaded only on this (rare) path
+    } else if (!M) {
+        // the grid geometry (launch constants here) is used only on this rare path
         Geo g;
         g.load(c, R);
         bool ok;
         const long long code = cell_code<DIM>(pi, g, ok);
         if (ok) {
-            visit_candidates<DIM, TPP>(F.start, g, code, shift_of<M>(st.f_shift), q, ff);
-            if (BOUND) visit_candidates<DIM, TPP>(B.start, g, code, shift_of<M>(st.b_shift), q, fb);
+            visit_candidates<DIM, TPP>(F.start, g, code, 0, q, ff);
+            if (BOUND) visit_candidates<DIM, TPP>(B.start, g, code, 0, q, fb);
+        }
+    } else {
+        // batched instances: the scene's geometry is re-read from the scene table
+        // at every row (volatile loads are not hoisted), so this rare path keeps
+        // no geometry in registers across the list walk above
+        bool ok;
+        long long code;
+        {
+            Geo g;
+            g.load(c, R);
+            code = cell_code<DIM>(pi, g, ok);
+        }
+        if (ok) {
+            visit_candidates_lean<DIM, TPP>(F.start, &c, R, code, st.f_shift, q, ff);
+            if (BOUND) visit_candidates_lean<DIM, TPP>(B.start, &c, R, code, st.b_shift, q, fb);
         }
     }
 }
