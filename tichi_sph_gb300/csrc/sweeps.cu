@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf 
     const float w0 = kw(0.f) * g.sig;
     if (ok) {
         // phase 1: record the pairs
-        visit_candidates<DIM>(F.start, g, code, f_shift, 0, [&](int j) {
+        visit_candidates_within<DIM>(F.start, g, pi, code, f_shift, 0, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf 
                 }
             }
         });
-        visit_candidates<DIM>(B.start, g, code, b_shift, 0, [&](int j) {
+        visit_candidates_within<DIM>(B.start, g, pi, code, b_shift, 0, [&](int j) {
             const float4 pj = B.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, 
     const long long code = cell_code<DIM>(pi, g, ok);
     float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f;
     if (ok) {
-        visit_candidates<DIM>(B.start, g, code, shift_of<M>(st.b_shift), 0, [&](int j) {
+        visit_candidates_within<DIM>(B.start, g, pi, code, shift_of<M>(st.b_shift), 0, [&](int j) {
             const float4 pj = B.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, 
                 comp += w * mv.y;
             }
         });
-        visit_candidates<DIM>(F.start, g, code, shift_of<M>(st.f_shift), 0, [&](int j) {
+        visit_candidates_within<DIM>(F.start, g, pi, code, shift_of<M>(st.f_shift), 0, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
