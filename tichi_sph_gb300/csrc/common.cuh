@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "../../include/tichi_sph.h"
 
 namespace tsph {
@@ -223,6 +225,13 @@ __device__ __forceinline__ float kwg(float q) {
 // per pair.  r^2 = 0 gives r = 0 and 1 / r = 0.
 __device__ __forceinline__ float pair_rinv(float r2, float &r) {
     const float inv = r2 > 0.f ? rsqrtf(r2) : 0.f;
+    r = r2 * inv;
+    return inv;
+}
+
+// pair_rinv for r^2 known to be positive (list entries).
+__device__ __forceinline__ float pair_rinv_pos(float r2, float &r) {
+    const float inv = rsqrtf(r2);
     r = r2 * inv;
     return inv;
 }
@@ -480,17 +489,24 @@ __device__ __forceinline__ void for_each_neighbor_tpp(const SceneConst &c, const
                                                       float4 pi, FF &&ff, FB &&fb) {
     const unsigned int pc = F.nbr_cnt[s];
     if (pc != kNbrOverflow) {
+        // list entries: the pair passed 0 < r^2 < h^2 when it was recorded (same
+        // positions, same FP32 arithmetic), so the callbacks may skip the test
         const int nfl = (int)(pc & 0xffffu), nbo = (int)(pc >> 16);
-        walk_blocks<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl, ff, fb);
-    } else if (!M) {
+        walk_blocks<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl,
+                         [&](int j) { ff(j, std::true_type{}); }, [&](int j) { fb(j, std::true_type{}); });
+        return;
+    }
+    auto ffs = [&](int j) { ff(j, std::false_type{}); };
+    auto fbs = [&](int j) { fb(j, std::false_type{}); };
+    if (!M) {
         // the grid geometry (launch constants here) is used only on this rare path
         Geo g;
         g.load(c, R);
         bool ok;
         const long long code = cell_code<DIM>(pi, g, ok);
         if (ok) {
-            visit_candidates<DIM, TPP>(F.start, g, code, 0, q, ff);
-            if (BOUND) visit_candidates<DIM, TPP>(B.start, g, code, 0, q, fb);
+            visit_candidates<DIM, TPP>(F.start, g, code, 0, q, ffs);
+            if (BOUND) visit_candidates<DIM, TPP>(B.start, g, code, 0, q, fbs);
         }
     } else {
         // batched instances: the scene's geometry is re-read from the scene table
@@ -504,8 +520,8 @@ __device__ __forceinline__ void for_each_neighbor_tpp(const SceneConst &c, const
             code = cell_code<DIM>(pi, g, ok);
         }
         if (ok) {
-            visit_candidates_lean<DIM, TPP>(F.start, &c, R, code, st.f_shift, q, ff);
-            if (BOUND) visit_candidates_lean<DIM, TPP>(B.start, &c, R, code, st.b_shift, q, fb);
+            visit_candidates_lean<DIM, TPP>(F.start, &c, R, code, st.f_shift, q, ffs);
+            if (BOUND) visit_candidates_lean<DIM, TPP>(B.start, &c, R, code, st.b_shift, q, fbs);
         }
     }
 }

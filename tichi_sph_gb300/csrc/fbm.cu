@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, Bound
             for (int q = 0; q < P; ++q) ui[q] = F.drift[q * F.cap + s];
             const float cc = c.fbm_c * dt, cd = dt * c.fbm_D, eps = 0.01f * g.h2;
             for_each_neighbor_tpp<DIM, false, 1, true>(c, st, k.R, F, B, s, 0, pi,
-                [&](int j) {
+                [&](int j, auto) {
                     const float4 pj = F.pos[j];
                     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                     const float r2 = dx * dx + dy * dy + dz * dz;
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, Bound
                         tmp[q] += (vfi[q] - vfj) * dif;
                     }
                 },
-                [&](int) {});
+                [&](int, auto) {});
         }
         bool neg = false;
 #pragma unroll

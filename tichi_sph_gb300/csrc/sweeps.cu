@@ -323,31 +323,25 @@ __global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B
     if (act) {
         pi = F.pos[s];
         vi = vin[s];
+        // IPPE_adv_psi pair term; list entries load both neighbour arrays at once
+        auto term = [&](const float4 *P, const float4 *V, int j, auto listed) {
+            constexpr bool L = decltype(listed)::value;
+            const float4 pj = P[j];
+            float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (L) vj = V[j];
+            const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (L || (r2 < g.h2 && r2 > 0.f)) {
+                if (!L) vj = V[j];
+                float r;
+                const float ri = L ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
+                const float f = kwg(r * g.inv_h) * g.sig_h * ri * pj.w;
+                acc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
+            }
+        };
         for_each_neighbor_tpp<DIM, true, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
-            [&](int j) {
-                const float4 pj = F.pos[j];
-                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < g.h2 && r2 > 0.f) {
-                    const float4 vj = vin[j];
-                    float r;
-                    const float ri = pair_rinv(r2, r);
-                    const float f = kwg(r * g.inv_h) * g.sig_h * ri * pj.w;
-                    acc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
-                }
-            },
-            [&](int j) {
-                const float4 pj = B.pos[j];
-                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < g.h2 && r2 > 0.f) {
-                    const float4 vj = B.vadv[j];
-                    float r;
-                    const float ri = pair_rinv(r2, r);
-                    const float f = kwg(r * g.inv_h) * g.sig_h * ri * pj.w;
-                    acc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
-                }
-            });
+            [&](int j, auto listed) { term(F.pos, vin, j, listed); },
+            [&](int j, auto listed) { term(B.pos, B.vadv, j, listed); });
     }
     acc = ln.sum(acc);
     double contrib = 0.0;
@@ -404,35 +398,27 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
             const float4 pi = F.pos[s];
             const float ki = F.kappa[s];
             const float Xi = pi.w;
+            // IPPE_update_vel_adv pair term; list entries load both neighbour arrays at once
+            auto term = [&](const float4 *P, const float *K, int j, auto listed) {
+                constexpr bool L = decltype(listed)::value;
+                const float4 pj = P[j];
+                float kj = 0.f;
+                if (L) kj = K[j];
+                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (L || (r2 < g.h2 && r2 > 0.f)) {
+                    if (!L) kj = K[j];
+                    float r;
+                    const float ri = L ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
+                    const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h * ri);
+                    ax += f * dx;
+                    ay += f * dy;
+                    az += f * dz;
+                }
+            };
             for_each_neighbor_tpp<DIM, true, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
-                [&](int j) {
-                    const float4 pj = F.pos[j];
-                    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 < g.h2 && r2 > 0.f) {
-                        const float kj = F.kappa[j];
-                        float r;
-                        const float ri = pair_rinv(r2, r);
-                        const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h * ri);
-                        ax += f * dx;
-                        ay += f * dy;
-                        az += f * dz;
-                    }
-                },
-                [&](int j) {
-                    const float4 pj = B.pos[j];
-                    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 < g.h2 && r2 > 0.f) {
-                        const float kj = B.kappa[j];
-                        float r;
-                        const float ri = pair_rinv(r2, r);
-                        const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h * ri);
-                        ax += f * dx;
-                        ay += f * dy;
-                        az += f * dz;
-                    }
-                });
+                [&](int j, auto listed) { term(F.pos, F.kappa, j, listed); },
+                [&](int j, auto listed) { term(B.pos, B.kappa, j, listed); });
         }
         ax = ln.sum(ax);
         ay = ln.sum(ay);
@@ -488,20 +474,24 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
     if (act) {
         const float4 pi = F.pos[s];
         for_each_neighbor_tpp<DIM, false, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
-            [&](int j) {
+            [&](int j, auto listed) {
+                constexpr bool L = decltype(listed)::value;
                 const float4 pj = F.pos[j];
+                float psij = 0.f;
+                if (L) psij = F.mpsi[j].y;
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < g.h2 && r2 > 0.f) {
+                if (L || (r2 < g.h2 && r2 > 0.f)) {
+                    if (!L) psij = F.mpsi[j].y;
                     float r;
-                    const float ri = pair_rinv(r2, r);
-                    const float f = -pj.w / F.mpsi[j].y * (kwg(r * g.inv_h) * g.sig_h) * ri;
+                    const float ri = L ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
+                    const float f = -pj.w / psij * (kwg(r * g.inv_h) * g.sig_h) * ri;
                     nx += f * dx;
                     ny += f * dy;
                     nz += f * dz;
                 }
             },
-            [&](int) {});
+            [&](int, auto) {});
     }
     nx = ln.sum(nx);
     ny = ln.sum(ny);
@@ -577,8 +567,30 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
             const long long code = cell_code<DIM>(pi, g, ok);
             if (ok) visit_candidates<DIM, TPP>(F.start, g, code, shift_of<M>(st.f_shift), ln.q, pair);
         } else {
-            for_each_neighbor_tpp<DIM, false, TPP, M>(c, st, k.R, F, B, s, ln.q, pi, pair,
-                                                   [&](int) {});
+            // viscosity only: list entries skip the range tests and load their
+            // neighbour's v_adv and psi together with its position
+            for_each_neighbor_tpp<DIM, false, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
+                [&](int j, auto listed) {
+                    constexpr bool L = decltype(listed)::value;
+                    if (!L) {
+                        pair(j);
+                        return;
+                    }
+                    const float4 pj = F.pos[j];
+                    const float4 vj = vin[j];
+                    const float psij = F.mpsi[j].y;
+                    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    float r;
+                    const float ri = pair_rinv_pos(r2, r);
+                    const float wg = kwg(r * g.inv_h) * g.sig_h;
+                    const float adx = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+                    const float f = lap * (pj.w / psij) * wg * ri * adx / (eps + r2);
+                    vx += f * dx;
+                    vy += f * dy;
+                    vz += f * dz;
+                },
+                [&](int, auto) {});
         }
     }
     vx = ln.sum(vx);

@@ -72,8 +72,8 @@ __global__ void __launch_bounds__(kBlock) k_wc_acce(KConst k, FluidBuf F, BoundB
         }
     };
     for_each_neighbor_tpp<DIM, true, 1, M>(c, st, k.R, F, B, s, 0, pi,
-        [&](int j) { term(F.pos[j], F.wcp[j].y, F.mv[j].x); },
-        [&](int j) { term(B.pos[j], B.wcp2[j], B.mv[j].x); });
+        [&](int j, auto) { term(F.pos[j], F.wcp[j].y, F.mv[j].x); },
+        [&](int j, auto) { term(B.pos[j], B.wcp2[j], B.mv[j].x); });
     const float4 a0 = F.acc[s];
     const float4 a = make_float4(a0.x + ax, a0.y + ay, a0.z + az, 0.f);
     F.acc[s] = a;
