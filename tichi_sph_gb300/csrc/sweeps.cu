@@ -58,23 +58,27 @@ __device__ __forceinline__ void publish_any(const KConst &k, int SceneStep::*fie
 // coincident particles -- go straight into W / rho / compression), then the
 // recorded list is walked for the kernel arithmetic.  A particle whose pairs do
 // not fit the list redoes the scan with the arithmetic inline.
-template <int DIM>
+// L (list entries, 0 < r < h known): mass / volume load beside the position,
+// no range tests; same arithmetic.
+template <int DIM, bool L = false>
 __device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf &F, float4 pi, int j, float &wsum,
                                                    float &rho, float &comp, float &a1x, float &a1y, float &a1z,
                                                    float &a2) {
     const float4 pj = F.pos[j];
+    float2 mv = make_float2(0.f, 0.f);
+    if (L) mv = F.mv[j];
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < g.h2) {
-        const float2 mv = F.mv[j];
+    if (L || r2 < g.h2) {
+        if (!L) mv = F.mv[j];
         float r;
-        const float ri = pair_rinv(r2, r);
+        const float ri = L ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
         const float q = r * g.inv_h;
         const float w = kw(q) * g.sig;
         wsum += w;
         rho += w * mv.x;
         comp += w * mv.y;
-        if (r2 > 0.f) {
+        if (L || r2 > 0.f) {
             const float wg = kwg(q) * g.sig_h;
             const float f = pj.w * wg * ri;
             a1x += f * dx;
@@ -85,22 +89,24 @@ __device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf 
     }
 }
 
-template <int DIM>
+template <int DIM, bool L = false>
 __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf &B, float4 pi, int j, float &wsum,
                                                    float &rho, float &comp, float &a1x, float &a1y, float &a1z) {
     const float4 pj = B.pos[j];
+    float2 mv = make_float2(0.f, 0.f);
+    if (L) mv = B.mv[j];
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < g.h2) {
-        const float2 mv = B.mv[j];
+    if (L || r2 < g.h2) {
+        if (!L) mv = B.mv[j];
         float r;
-        const float ri = pair_rinv(r2, r);
+        const float ri = L ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
         const float q = r * g.inv_h;
         const float w = kw(q) * g.sig;
         wsum += w;
         rho += w * mv.x;
         comp += w * mv.y;
-        if (r2 > 0.f) {
+        if (L || r2 > 0.f) {
             const float f = pj.w * kwg(q) * g.sig_h * ri;
             a1x += f * dx;
             a1y += f * dy;
@@ -167,8 +173,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf 
         if (nfl + nbo <= cap) {
             // phase 2: the arithmetic over the recorded pairs
             walk_blocks<1>(F.nbr, s, stride, 0, nfl, nfl + nbo,
-                [&](int j) { density_pair_fluid<DIM>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2); },
-                [&](int j) { density_pair_bound<DIM>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z); });
+                [&](int j) { density_pair_fluid<DIM, true>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2); },
+                [&](int j) { density_pair_bound<DIM, true>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z); });
         } else {
             // list overflow: one scan with the arithmetic inline
             wsum = rho = comp = a2 = a1x = a1y = a1z = 0.f;
