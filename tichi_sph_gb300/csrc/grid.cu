@@ -232,6 +232,11 @@ __device__ __forceinline__ void insertion_sort(int *p, long long beg, long long 
     }
 }
 
+// Cells of up to kRegSort particles are sorted in registers: all ids load at
+// once (independent loads, one memory latency), a fixed odd-even transposition
+// network orders them, one write-back; larger cells use insertion_sort.
+constexpr int kRegSort = 16;
+
 __global__ void __launch_bounds__(kBlock) k_cell_sort(KConst k, const int *__restrict__ fstart, int *fperm,
                                                       const int *__restrict__ bstart, int *bperm) {
     const int g = blockIdx.y;
@@ -239,10 +244,30 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(KConst k, const int *__res
     if (c >= k.total_nodes) return;
     const int *start = g ? bstart : fstart;
     const int beg = start[c], end = start[c + 1];
-    if (end - beg < 2) return;
+    const int n = end - beg;
+    if (n < 2) return;
     const int sc = scene_of_cell(k, c);
     const long long shift = g ? k.ss[sc].b_shift : k.ss[sc].f_shift;
-    insertion_sort(g ? bperm : fperm, beg + shift, end + shift);
+    int *p = (g ? bperm : fperm) + beg + shift;
+    if (n > kRegSort) {
+        insertion_sort(p, 0, n);
+        return;
+    }
+    int v[kRegSort];
+#pragma unroll
+    for (int i = 0; i < kRegSort; ++i) v[i] = i < n ? p[i] : 0x7fffffff;
+#pragma unroll
+    for (int r = 0; r < kRegSort; ++r) {
+#pragma unroll
+        for (int i = r & 1; i + 1 < kRegSort; i += 2) {
+            const int a = min(v[i], v[i + 1]), b = max(v[i], v[i + 1]);
+            v[i] = a;
+            v[i + 1] = b;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kRegSort; ++i)
+        if (i < n) p[i] = v[i];
 }
 
 // Each scene's particles without a valid cell, ordered by id (one thread per scene).
