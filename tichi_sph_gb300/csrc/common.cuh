@@ -314,7 +314,8 @@ __device__ __forceinline__ void visit_candidates_lean(const int *__restrict__ st
 
 // visit_candidates for callers that use only candidates with r < h: template
 // rows whose y/z slab is farther than h from the particle are skipped (the
-// corner rows (dy, dz) = (+-1, +-1) for about a fifth of the particles each).
+// corner rows (dy, dz) = (+-1, +-1) for about a fifth of the particles each),
+// and so are a kept row's end cells whose box lies farther than h.
 // The test keeps a 1e-5 relative margin, so every skipped candidate fails the
 // FP32 r^2 < h^2 test as well; a row's x-wrapped cells (the reference's linear
 // codes) are even farther away.
@@ -323,17 +324,30 @@ __device__ __forceinline__ void visit_candidates_within(const int *__restrict__ 
                                                         long long code, long long shift, int q, F &&f) {
     const int R = g.R;
     const int zr = (DIM == 3) ? R : 0;
-    // distance of the particle to its cell's lower / upper faces in y and z
+    // distance of the particle to its cell's lower / upper faces in x, y and z
+    const float qx = __fdiv_rn(p.x - g.lb[0], g.h);
     const float qy = __fdiv_rn(p.y - g.lb[1], g.h), qz = DIM == 3 ? __fdiv_rn(p.z - g.lb[2], g.h) : 0.f;
-    const float fy = qy - floorf(qy), fz = qz - floorf(qz);
+    const float fx = qx - floorf(qx), fy = qy - floorf(qy), fz = qz - floorf(qz);
     const float skip2 = g.h2 * (1.f + 1e-5f);
     for (int dz = -zr; dz <= zr; ++dz) {
         const float ez = dz == 0 ? 0.f : (dz < 0 ? fz + (float)(-dz - 1) : (1.f - fz) + (float)(dz - 1)) * g.h;
         for (int dy = -R; dy <= R; ++dy) {
             const float ey = dy == 0 ? 0.f : (dy < 0 ? fy + (float)(-dy - 1) : (1.f - fy) + (float)(dy - 1)) * g.h;
-            if (ey * ey + ez * ez > skip2) continue;
+            const float eyz = ey * ey + ez * ez;
+            if (eyz > skip2) continue;
             long long rc = code + dy * g.nx + dz * g.nxny;
             long long lo = rc - R, hi = rc + R;
+            // the row's end cells that lie farther than h (in x together with y / z)
+            for (int dx = -R; dx < 0; ++dx) {
+                const float ex = (fx + (float)(-dx - 1)) * g.h;
+                if (eyz + ex * ex > skip2) lo = rc + dx + 1;
+                else break;
+            }
+            for (int dx = R; dx > 0; --dx) {
+                const float ex = ((1.f - fx) + (float)(dx - 1)) * g.h;
+                if (eyz + ex * ex > skip2) hi = rc + dx - 1;
+                else break;
+            }
             if (lo < 1) lo = 1;
             if (hi > g.node_num - 1) hi = g.node_num - 1;
             if (lo > hi) continue;
