@@ -116,7 +116,7 @@ __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf 
 }
 
 template <int DIM, bool M>
-__global__ void __launch_bounds__(kBlock, 4) k_density_fluid(KConst k, FluidBuf F, BoundBuf B) {
+__global__ void __launch_bounds__(kBlock, 5) k_density_fluid(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int sc = f_block_scene<M>(k, blockIdx.x * (int64_t)kBlock);
     const SceneConst &c = scene<M>(k, sc);
@@ -308,7 +308,7 @@ __global__ void k_solve_begin(KConst k, int kind, int flip, cudaGraphConditional
 // and, through the scene's last block, to its psi_sum (block order:
 // deterministic).
 template <int DIM, int TPP, bool M>
-__global__ void __launch_bounds__(kBlock) k_psi(KConst k, FluidBuf F, BoundBuf B, double *partials) {
+__global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBuf B, double *partials) {
     __shared__ double sh[kBlock / 32];
     __shared__ unsigned int arrived;
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
