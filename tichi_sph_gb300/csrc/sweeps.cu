@@ -116,7 +116,7 @@ __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf 
 }
 
 template <int DIM, bool M>
-__global__ void __launch_bounds__(kBlock, 5) k_density_fluid(KConst k, FluidBuf F, BoundBuf B) {
+__global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int sc = f_block_scene<M>(k, blockIdx.x * (int64_t)kBlock);
     const SceneConst &c = scene<M>(k, sc);
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_density_fluid(KConst k, FluidBuf 
 // The boundary's own sums: SPH_prepare_attr (b,b)(b,f), SPH_prepare_alpha_2 (b,f),
 // SPH_prepare_alpha (sph.py:50-105 as called by main.py:190-197).
 template <int DIM, bool M>
-__global__ void __launch_bounds__(kBlock) k_density_bound(KConst k, FluidBuf F, BoundBuf B) {
+__global__ void __launch_bounds__(kBlock, 6) k_density_bound(KConst k, FluidBuf F, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int sc = b_block_scene<M>(k, blockIdx.x * (int64_t)kBlock);
     const SceneConst &c = scene<M>(k, sc);
