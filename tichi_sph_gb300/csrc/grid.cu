@@ -20,6 +20,11 @@ template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_cfl(KConst k, const float *__restrict__ vel, int64_t n) {
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * kBlock;
+    // each warp keeps its running maximum for the scene it last saw and issues
+    // one atomic when the scene changes (and at the end): one atomic per warp
+    // for a one-scene context instead of one per warp and iteration
+    int wsc = -1;
+    float wmax = 0.f;
     for (int64_t base = blockIdx.x * (int64_t)kBlock; base < n; base += stride) {
         const int64_t i = base + threadIdx.x;
         const bool act = i < n;
@@ -37,15 +42,23 @@ __global__ void __launch_bounds__(kBlock) k_cfl(KConst k, const float *__restric
             sc = k.f_user_scene[i];
         }
         const int sc0 = __shfl_sync(0xffffffffu, sc, 0);
+        if (sc0 < 0) continue;  // no particle left in this warp
         if (__all_sync(0xffffffffu, !act || sc == sc0)) {
             float m = vn;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-            if (lane == 0 && m > 0.f) atomicMax(&k.ss[sc0].vmax_bits, __float_as_uint(m));
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (sc0 != wsc) {
+                if (lane == 0 && wsc >= 0 && wmax > 0.f) atomicMax(&k.ss[wsc].vmax_bits, __float_as_uint(wmax));
+                wsc = sc0;
+                wmax = m;
+            } else {
+                wmax = fmaxf(wmax, m);
+            }
         } else if (act && vn > 0.f) {
             atomicMax(&k.ss[sc].vmax_bits, __float_as_uint(vn));
         }
     }
+    if (lane == 0 && wsc >= 0 && wmax > 0.f) atomicMax(&k.ss[wsc].vmax_bits, __float_as_uint(wmax));
     if (last_block_done(&k.dg->ticket[kGtCfl], gridDim.x)) {
         for (int s = threadIdx.x; s < k.n_scenes; s += kBlock) {
             const SceneConst &c = k.sc[s];
