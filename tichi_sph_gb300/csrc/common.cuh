@@ -229,6 +229,9 @@ __device__ __forceinline__ float pair_rinv(float r2, float &r) {
     return inv;
 }
 
+// The density sweeps' per-pair quotient uses __fdividef (two instructions,
+// within 2 ulp) instead of an IEEE division: far inside the 1e-5 tolerance.
+
 // pair_rinv for r^2 known to be positive (list entries).
 __device__ __forceinline__ float pair_rinv_pos(float r2, float &r) {
     const float inv = rsqrtf(r2);

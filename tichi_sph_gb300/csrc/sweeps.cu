@@ -84,7 +84,7 @@ __device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf 
             a1x += f * dx;
             a1y += f * dy;
             a1z += f * dz;
-            a2 += wg * wg * pj.w * pj.w / mv.x;
+            a2 += __fdividef(wg * wg * pj.w * pj.w, mv.x);
         }
     }
 }
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_bound(KConst k, FluidBuf 
                 comp += w * mv.y;
                 if (r2 > 0.f) {
                     const float wg = kwg(q) * g.sig_h;
-                    a2 += wg * wg * pj.w * pj.w / mv.x;
+                    a2 += __fdividef(wg * wg * pj.w * pj.w, mv.x);
                 }
             }
         });
