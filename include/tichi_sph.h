@@ -185,7 +185,8 @@ int tsph_set_state(tsph_ctx *ctx, double time_count, float dt, double compressio
 /* Debug / parity: builds the grid for the current positions and writes, per
  * particle in caller order, the number of neighbours with 0 < r < h among the
  * fluid ([0]) and the boundary ([1]) set, and an order-independent 64-bit hash
- * of that neighbour set.  fluid_out: int32[n_f][2] + uint64[n_f]; bound_out the
+ * of that neighbour set, as found by the candidate scan that records the
+ * step's neighbour pairs (it skips template rows and cells beyond h).  fluid_out: int32[n_f][2] + uint64[n_f]; bound_out the
  * same for the boundary set.  Synchronises. */
 int tsph_neighbor_stats(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound,
                         int32_t *fluid_counts, uint64_t *fluid_hash,

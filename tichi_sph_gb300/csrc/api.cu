@@ -305,6 +305,8 @@ void make_scene(const tsph_params &p, SceneConst &c) {
     c.wc_gamma = p.wc_gamma;
     c.div_tol = p.divergence_threshold;
     c.comp_tol = p.compression_threshold;
+    const long long span = 2ll * p.neighb_range;
+    c.row_trim = p.grid_size[0] > span && (p.dim == 2 || p.grid_size[1] > span);
 }
 
 int check_params(const tsph_params &p) {

@@ -44,6 +44,9 @@ struct SceneConst {
     float part_size, cfl;
     int cs, iter_min, iter_max, fbm_max_passes, wc_gamma;
     float div_tol, comp_tol;
+    // 1 when a template row cannot alias another (nx > 2r, and ny > 2r in 3D):
+    // only then may candidates be skipped by their cell's geometry
+    int row_trim;
     // caller order [f_user, f_user + f_n); sorted slots [f_slot, f_slot + f_slots)
     long long f_user, f_n, f_slot, f_slots;
     long long b_user, b_n, b_slot, b_slots;
@@ -134,7 +137,7 @@ struct Geo {
     float lb[3];
     float h, h2, inv_h, sig, sig_h;
     long long node_num, nx, nxny, cbase;
-    int R;
+    int R, row_trim;
     __device__ __forceinline__ void load(const SceneConst &c, int R_) {
         lb[0] = c.lb[0];
         lb[1] = c.lb[1];
@@ -149,6 +152,7 @@ struct Geo {
         nxny = c.nxny;
         cbase = c.cbase;
         R = R_;
+        row_trim = c.row_trim;
     }
 };
 
@@ -318,10 +322,18 @@ __device__ __forceinline__ void visit_candidates_lean(const int *__restrict__ st
 // visit_candidates for callers that use only candidates with r < h: template
 // rows whose y/z slab is farther than h from the particle are skipped (the
 // corner rows (dy, dz) = (+-1, +-1) for about a fifth of the particles each),
-// and so are a kept row's end cells whose box lies farther than h.
-// The test keeps a 1e-5 relative margin, so every skipped candidate fails the
-// FP32 r^2 < h^2 test as well; a row's x-wrapped cells (the reference's linear
-// codes) are even farther away.
+// and so are a kept row's end cells whose box lies farther than h.  The rest of
+// a row is one contiguous range visited in order, as in visit_candidates.
+//
+// Exactness: a candidate within h of the particle lies at most one cell away
+// on every axis, so with nx, ny > 2r it sits in the template cell of its
+// geometric offset and the face distances below bound its distance; a wrapped
+// or outside particle found through another template cell is farther than h
+// and fails the test either way.  The face distances come from FP32 cell
+// coordinates whose rounding grows with the coordinate (~1.2e-7 cells per cell
+// of distance from lb, for the particle and for the candidate's own cell), so
+// the margin on h^2 grows with it too.  Without row_trim (a row could alias
+// another) the margin is infinite: every candidate is visited.
 template <int DIM, int TPP = 1, class F>
 __device__ __forceinline__ void visit_candidates_within(const int *__restrict__ start, const Geo &g, float4 p,
                                                         long long code, long long shift, int q, F &&f) {
@@ -331,7 +343,8 @@ __device__ __forceinline__ void visit_candidates_within(const int *__restrict__ 
     const float qx = __fdiv_rn(p.x - g.lb[0], g.h);
     const float qy = __fdiv_rn(p.y - g.lb[1], g.h), qz = DIM == 3 ? __fdiv_rn(p.z - g.lb[2], g.h) : 0.f;
     const float fx = qx - floorf(qx), fy = qy - floorf(qy), fz = qz - floorf(qz);
-    const float skip2 = g.h2 * (1.f + 1e-5f);
+    const float qm = fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz))) + (float)(R + 1);
+    const float skip2 = g.row_trim ? g.h2 * (1.f + 1e-5f + 2e-6f * (float)R * qm) : __int_as_float(0x7f800000);
     for (int dz = -zr; dz <= zr; ++dz) {
         const float ez = dz == 0 ? 0.f : (dz < 0 ? fz + (float)(-dz - 1) : (1.f - fz) + (float)(dz - 1)) * g.h;
         for (int dy = -R; dy <= R; ++dy) {

@@ -501,7 +501,9 @@ __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, 
     int cf = 0, cb = 0;
     uint64_t hsum = 0;
     if (ok) {
-        visit_candidates<DIM>(F.start, g, code, st.f_shift, 0, [&](int j) {
+        // the density sweep's visitor (it records the pairs every later sweep
+        // walks): its skipped rows and cells must hold no pair with r < h
+        visit_candidates_within<DIM>(F.start, g, pi, code, st.f_shift, 0, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
@@ -510,7 +512,7 @@ __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, 
                 hsum += mix64((uint64_t)(uint32_t)F.perm[j]);
             }
         });
-        visit_candidates<DIM>(B.start, g, code, st.b_shift, 0, [&](int j) {
+        visit_candidates_within<DIM>(B.start, g, pi, code, st.b_shift, 0, [&](int j) {
             const float4 pj = B.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
