@@ -508,6 +508,47 @@ __device__ __forceinline__ void walk_blocks(const int *__restrict__ nbr, int64_t
     }
 }
 
+// Entries [lo, hi) of the blocked list in whole four-entry blocks, for lane q
+// (blocks b = q mod TPP): all four callbacks of a block run unconditionally,
+// f(j, valid), an entry outside [lo, hi) with valid = false and the index of the
+// block's first entry in range, so the block's gathers carry no branch and can
+// all be issued before the first one is used.  Per lane, the valid entries come
+// in the same order as in walk_blocks.
+template <int TPP, class Fn>
+__device__ __forceinline__ void walk_range_pred(const int4 *__restrict__ L4, int64_t cap, int q, int lo, int hi,
+                                                Fn &&f) {
+    if (lo >= hi) return;
+    const int b0 = lo >> 2, b1 = (hi + 3) >> 2;
+    int b = b0 + ((q - b0) & (TPP - 1));
+    if (b >= b1) return;
+    int4 cur = __ldg(L4 + (int64_t)b * cap);
+    while (b < b1) {
+        const int bn = b + TPP;
+        int4 nxt = cur;
+        if (bn < b1) nxt = __ldg(L4 + (int64_t)bn * cap);
+        const int t0 = b << 2;
+        const int first = lo > t0 ? lo - t0 : 0;  // first in-range entry (0..3)
+        const int jf = first == 0 ? cur.x : first == 1 ? cur.y : first == 2 ? cur.z : cur.w;
+        const int jj[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int t = t0 + e;
+            const bool v = t >= lo && t < hi;
+            f(v ? jj[e] : jf, v);
+        }
+        cur = nxt;
+        b = bn;
+    }
+}
+
+template <int TPP, class FF, class FB>
+__device__ __forceinline__ void walk_blocks_pred(const int *__restrict__ nbr, int64_t s, int64_t cap, int q,
+                                                 int nfl, int ntot, FF &&ff, FB &&fb) {
+    const int4 *L4 = reinterpret_cast<const int4 *>(nbr) + s;
+    walk_range_pred<TPP>(L4, cap, q, 0, nfl, ff);
+    walk_range_pred<TPP>(L4, cap, q, nfl, ntot, fb);
+}
+
 // Neighbours of sorted fluid particle s for lane q of a TPP-lane particle group:
 // the blocked list, or -- for a particle whose list overflowed -- the strided
 // candidate scan of the template cells.  Both visit the pairs the density sweep
@@ -522,12 +563,25 @@ __device__ __forceinline__ void for_each_neighbor_tpp(const SceneConst &c, const
         // list entries: the pair passed 0 < r^2 < h^2 when it was recorded (same
         // positions, same FP32 arithmetic), so the callbacks may skip the test
         const int nfl = (int)(pc & 0xffffu), nbo = (int)(pc >> 16);
-        walk_blocks<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl,
-                         [&](int j) { ff(j, std::true_type{}); }, [&](int j) { fb(j, std::true_type{}); });
+        if constexpr (std::is_invocable_v<FF &, int, std::true_type, bool>) {
+            // callbacks that take a valid flag: branch-free four-entry blocks
+            walk_blocks_pred<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl,
+                                  [&](int j, bool v) { ff(j, std::true_type{}, v); },
+                                  [&](int j, bool v) { fb(j, std::true_type{}, v); });
+        } else {
+            walk_blocks<TPP>(F.nbr, s, F.cap, q, nfl, BOUND ? nfl + nbo : nfl,
+                             [&](int j) { ff(j, std::true_type{}); }, [&](int j) { fb(j, std::true_type{}); });
+        }
         return;
     }
-    auto ffs = [&](int j) { ff(j, std::false_type{}); };
-    auto fbs = [&](int j) { fb(j, std::false_type{}); };
+    auto ffs = [&](int j) {
+        if constexpr (std::is_invocable_v<FF &, int, std::false_type, bool>) ff(j, std::false_type{}, true);
+        else ff(j, std::false_type{});
+    };
+    auto fbs = [&](int j) {
+        if constexpr (std::is_invocable_v<FB &, int, std::false_type, bool>) fb(j, std::false_type{}, true);
+        else fb(j, std::false_type{});
+    };
     if (!M) {
         // the grid geometry (launch constants here) is used only on this rare path
         Geo g;

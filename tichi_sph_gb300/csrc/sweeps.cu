@@ -345,6 +345,8 @@ __global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBu
                 acc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
             }
         };
+        // branchy list walk: two float4 gathers per entry leave no registers
+        // for a whole block's gathers at six blocks per SM
         for_each_neighbor_tpp<DIM, true, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
             [&](int j, auto listed) { term(F.pos, vin, j, listed); },
             [&](int j, auto listed) { term(B.pos, B.vadv, j, listed); });
@@ -405,7 +407,8 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
             const float ki = F.kappa[s];
             const float Xi = pi.w;
             // IPPE_update_vel_adv pair term; list entries load both neighbour arrays at once
-            auto term = [&](const float4 *P, const float *K, int j, auto listed) {
+            // (valid = false: a padding call of a list block, computed and dropped)
+            auto term = [&](const float4 *P, const float *K, int j, auto listed, bool valid) {
                 constexpr bool L = decltype(listed)::value;
                 const float4 pj = P[j];
                 float kj = 0.f;
@@ -417,14 +420,14 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
                     float r;
                     const float ri = L ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
                     const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h * ri);
-                    ax += f * dx;
-                    ay += f * dy;
-                    az += f * dz;
+                    ax = valid ? ax + f * dx : ax;
+                    ay = valid ? ay + f * dy : ay;
+                    az = valid ? az + f * dz : az;
                 }
             };
             for_each_neighbor_tpp<DIM, true, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
-                [&](int j, auto listed) { term(F.pos, F.kappa, j, listed); },
-                [&](int j, auto listed) { term(B.pos, B.kappa, j, listed); });
+                [&](int j, auto listed, bool v) { term(F.pos, F.kappa, j, listed, v); },
+                [&](int j, auto listed, bool v) { term(B.pos, B.kappa, j, listed, v); });
         }
         ax = ln.sum(ax);
         ay = ln.sum(ay);
