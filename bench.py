@@ -57,6 +57,43 @@ ALGO_BYTES_3D = {
 }
 
 
+# FP32 operations per evaluation in the neighbour sweeps, counted from the CUDA
+# source (add / mul 1, FMA 2, rsqrt 1; both spline branches are evaluated):
+# a candidate test (dx, r^2) 8; a fluid particle's pair in the density sweep's
+# list pass 50 with a fluid neighbour, 44 with a boundary one (it recomputes the
+# test); a boundary particle's pair beyond its candidate test 19 with a boundary
+# neighbour, 34 with a fluid one; a list pair in psi 32 and in vel 31.
+FLOPS = {"cand": 8, "dens_ff": 50, "dens_fb": 44, "dens_bb": 19, "dens_bf": 34, "psi": 32, "vel": 31}
+
+
+def alu_roofline(solver, ph, top):
+    """Secondary (arithmetic) roofline of the neighbour sweeps: FP32 operations
+    per launch from the exact pair and candidate counts of the current state,
+    over the launch time, against the GPU's FMA rate measured here."""
+    from tichi_sph_gb300.sph import fp32_fma_peak
+    fc, _, bc, _ = solver.neighbor_stats()
+    cf, cb = solver.candidate_stats()
+    ff, fb = int(fc[:, 0].sum()), int(fc[:, 1].sum())
+    bf, bb = int(bc[:, 0].sum()), int(bc[:, 1].sum())
+    cand = int(cf.sum()) + int(cb.sum())
+    flops = {
+        "density": FLOPS["cand"] * cand + FLOPS["dens_ff"] * ff + FLOPS["dens_fb"] * fb + FLOPS["dens_bb"] * bb
+        + FLOPS["dens_bf"] * bf,
+        "psi": FLOPS["psi"] * (ff + fb),
+        "vel": FLOPS["vel"] * (ff + fb),
+    }
+    peak = fp32_fma_peak()
+    per = {k: flops[k] / (ph[k] * 1e-3) / 1e12 for k in flops}
+    k = top if top in flops else max(flops, key=lambda x: ph[x])
+    return {"bound": "fp32", "kernel": k, "achieved": per[k], "peak": peak, "unit": "TFLOP/s",
+            "frac": per[k] / peak, "peak_source": "measured by bench.py on this GPU (FMA chains, tsph_fp32_fma_peak)",
+            "flops_per_launch": flops, "achieved_per_phase": per, "frac_per_phase": {x: per[x] / peak for x in per},
+            "pairs_per_step": {"fluid_fluid": ff, "fluid_boundary": fb, "boundary_fluid": bf,
+                               "boundary_boundary": bb},
+            "density_candidates_per_launch": cand,
+            "flops_per_evaluation": FLOPS}
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
@@ -551,6 +588,10 @@ def main():
                 "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": ph[top],
                 "phase_ms_per_launch": ph, "phase_share_of_step": {k: share[k] / sum(share.values()) for k in share}}
 
+    alu = None
+    if not args.no_profile:
+        alu = alu_roofline(solver, ph, top)
+
     # end to end through the public API with host buffers
     e2e = None
     if not args.no_e2e:
@@ -616,6 +657,7 @@ def main():
                        "graph": "host-driven solver loops" if args.hostloop else
                        "one CUDA graph per substep, device-side while nodes"},
             "roofline": roofline,
+            "alu_roofline": alu,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,

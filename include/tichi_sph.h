@@ -192,6 +192,18 @@ int tsph_neighbor_stats(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bo
                         int32_t *fluid_counts, uint64_t *fluid_hash,
                         int32_t *bound_counts, uint64_t *bound_hash, void *stream);
 
+/* Measurement: the number of candidates the density sweep's scan visits per
+ * particle (caller order) in the fluid grid ([0]) and the boundary grid ([1]),
+ * for the current positions; fluid_counts int32[n_f][2], bound_counts
+ * int32[n_b][2].  Synchronises. */
+int tsph_candidate_stats(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound,
+                         int32_t *fluid_counts, int32_t *bound_counts, void *stream);
+
+/* Measurement: the FP32 FMA rate of the current GPU in TFLOP/s (independent
+ * fused multiply-add chains on every SM, an FMA counted as two operations),
+ * timed with CUDA events on `stream`; synchronises.  Needs no context. */
+int tsph_fp32_fma_peak(double *tflops_out, void *stream);
+
 /* Measurement: runs each phase of a step `reps` times back to back on `stream`
  * and writes its mean duration per launch in milliseconds (CUDA events on that
  * stream) to ms_out[TSPH_PH_COUNT].  The phases leave the particle state as one

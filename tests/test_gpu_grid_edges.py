@@ -1,5 +1,5 @@
-"""Neighbour sets on grid shapes where the reference's linear cell codes alias
-(needs a GPU).
+"""Neighbour sets on grid shapes where the reference's linear cell codes alias,
+and the measurement entry points (needs a GPU).
 
 The density sweep's candidate scan skips template rows and cells whose
 geometry lies farther than h.  That is exact only when no template row can
@@ -89,3 +89,51 @@ def test_neighbour_sets_on_narrow_grids(dim, nx_cells):
         doubled += len(pr.i) - len(set(zip(pr.i.tolist(), pr.j.tolist())))
     # the aliasing case really revisits cells; the other does not
     assert (doubled > 0) == (nx_cells == 2)
+
+
+@pytest.mark.parametrize("nx_cells", [2, 3])
+def test_candidate_counts(nx_cells):
+    """tsph_candidate_stats: without skipping (aliasing rows) the scan visits
+    exactly the reference template's candidates; with skipping, a subset of
+    them that still holds every pair within h."""
+    _need_cuda()
+    from tests.test_gpu_parity import _oracle_neighbours
+    from tichi_sph_gb300 import Fluid, Solver, sph_config
+    dim = 3
+    cfg_d, scen, span = _scene(dim, nx_cells)
+    cfg = sph_config.Config(cfg_d, scen)
+    rng = np.random.default_rng(7 + nx_cells)
+    pos = {"fluid": _cloud(rng, 600, dim, span), "bound": _cloud(rng, 200, dim, span)}
+    sets = []
+    for uid, name in enumerate(("fluid", "bound")):
+        o = Fluid(len(pos[name]), cfg, uid, device="cuda")
+        o.part_num[None] = len(pos[name])
+        o.pos[:len(pos[name])] = torch.as_tensor(pos[name], device="cuda")
+        o.mass[:len(pos[name])] = 1.0
+        o.rest_volume[:len(pos[name])] = 1e-3
+        sets.append(o)
+    solver = Solver(cfg, sets[0], sets[1])
+    cf, cb = [t.cpu().numpy() for t in solver.candidate_stats()]
+    solver.close()
+    p = O.Params.from_config(cfg_d, scen, taichi_f32=True)
+    arr = lambda x: {"pos": x.astype(np.float64)}
+    ofl, obd = O.sets_from_arrays(p, arr(pos["fluid"]), arr(pos["bound"]))
+    grid = O.Grid(p, [ofl, obd])
+    for obj, cnt in ((ofl, cf), (obd, cb)):
+        for col, nobj, bits in ((0, ofl, 0), (1, obd, 1 << 32)):
+            tmpl = np.bincount(grid.pairs(obj, nobj).i, minlength=obj.n)
+            pairs, _, _ = _oracle_neighbours(p, obj, nobj, grid, bits)
+            if nx_cells == 2:
+                np.testing.assert_array_equal(cnt[:, col], tmpl)
+            else:
+                assert (cnt[:, col] <= tmpl).all() and (cnt[:, col] >= pairs).all()
+                assert cnt[:, col].sum() < tmpl.sum()
+
+
+def test_fp32_fma_peak_is_plausible():
+    _need_cuda()
+    from tichi_sph_gb300.sph import fp32_fma_peak
+    tf = fp32_fma_peak()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    # 128 FP32 lanes per SM, two operations per FMA, 0.5 - 3.5 GHz
+    assert sms * 128 * 2 * 0.5e9 / 1e12 < tf < sms * 128 * 2 * 3.5e9 / 1e12, tf

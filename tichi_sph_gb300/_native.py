@@ -83,6 +83,8 @@ SIGNATURES = {
     "tsph_set_state": (C.c_int, [CtxP, C.c_double, C.c_float, C.c_double, C.c_void_p]),
     "tsph_neighbor_stats": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), _ip, C.POINTER(C.c_uint64),
                                       _ip, C.POINTER(C.c_uint64), C.c_void_p]),
+    "tsph_candidate_stats": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), _ip, _ip, C.c_void_p]),
+    "tsph_fp32_fma_peak": (C.c_int, [C.POINTER(C.c_double), C.c_void_p]),
     "tsph_profile_phases": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_int, _fp, C.c_void_p]),
     "tsph_fluid_density_noalloc": (C.c_int, [C.POINTER(Params), _fp, _fp, _fp, _i64, _fp, _fp, _fp, _i64,
                                              _fp, _fp, _fp, C.c_void_p]),

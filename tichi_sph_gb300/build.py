@@ -16,7 +16,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libtichi_sph.so")
-SOURCES = ["grid.cu", "sweeps.cu", "fbm.cu", "api.cu", "noalloc.cu", "adjoint.cu", "wcsph.cu"]
+SOURCES = ["grid.cu", "sweeps.cu", "fbm.cu", "api.cu", "noalloc.cu", "adjoint.cu", "wcsph.cu", "measure.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 

@@ -749,7 +749,21 @@ int tsph_neighbor_stats(tsph_ctx *c, const tsph_set *f, const tsph_set *b, int32
     cudaStream_t st = (cudaStream_t)stream;
     launch_step_begin(*c, st);
     launch_grid_build(*c, *f, *b, st);
-    launch_neighbor_stats(*c, fc, fh, bc, bh, st);
+    launch_neighbor_stats(*c, fc, fh, bc, bh, 0, st);
+    TSPH_CK(cudaGetLastError());
+    TSPH_CK(cudaStreamSynchronize(st));
+    return TSPH_OK;
+}
+
+int tsph_candidate_stats(tsph_ctx *c, const tsph_set *f, const tsph_set *b, int32_t *fc, int32_t *bc,
+                         void *stream) {
+    if (!fc || !bc) return fail(TSPH_ERR_INVALID, "null output");
+    int rc = bind_sets(c, f, b);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    launch_step_begin(*c, st);
+    launch_grid_build(*c, *f, *b, st);
+    launch_neighbor_stats(*c, fc, nullptr, bc, nullptr, 1, st);
     TSPH_CK(cudaGetLastError());
     TSPH_CK(cudaStreamSynchronize(st));
     return TSPH_OK;

@@ -39,7 +39,8 @@ void launch_step_begin(tsph_ctx &c, cudaStream_t st);
 void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st);
 void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);
 void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);
-void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, uint64_t *bh, cudaStream_t st);
+void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, uint64_t *bh, int cand,
+                           cudaStream_t st);
 
 // sweeps.cu
 void launch_density(tsph_ctx &c, cudaStream_t st);

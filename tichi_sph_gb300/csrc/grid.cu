@@ -483,9 +483,12 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
     return x ^ (x >> 31);
 }
 
+// Per particle: its neighbours with 0 < r < h in each set (FP32 q < 1, as the
+// reference tests) and their order-independent hash, or -- cand != 0 -- the
+// number of candidates the density sweep's scan visits in each grid (no hash).
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, FluidBuf F, BoundBuf B,
-                                                           int32_t *counts, uint64_t *hash) {
+                                                           int32_t *counts, uint64_t *hash, int cand) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int64_t cap = bound ? B.cap : F.cap;
     if (s >= cap) return;
@@ -507,7 +510,9 @@ __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, 
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 > 0.f && sqrtf(r2) * g.inv_h < 1.f) {
+            if (cand) {
+                ++cf;
+            } else if (r2 > 0.f && sqrtf(r2) * g.inv_h < 1.f) {
                 ++cf;
                 hsum += mix64((uint64_t)(uint32_t)F.perm[j]);
             }
@@ -516,7 +521,9 @@ __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, 
             const float4 pj = B.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 > 0.f && sqrtf(r2) * g.inv_h < 1.f) {
+            if (cand) {
+                ++cb;
+            } else if (r2 > 0.f && sqrtf(r2) * g.inv_h < 1.f) {
                 ++cb;
                 hsum += mix64((1ull << 32) | (uint64_t)(uint32_t)B.perm[j]);
             }
@@ -525,7 +532,7 @@ __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, 
     const int pid = bound ? B.perm[s] : F.perm[s];
     counts[2 * pid] = cf;
     counts[2 * pid + 1] = cb;
-    hash[pid] = hsum;
+    if (hash) hash[pid] = hsum;
 }
 
 // ----------------------------------------------------------------------------- launchers
@@ -596,13 +603,14 @@ void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream
     }
 }
 
-void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, uint64_t *bh, cudaStream_t st) {
+void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, uint64_t *bh, int cand,
+                           cudaStream_t st) {
     if (c.k.dim == 3) {
-        k_neighbor_stats<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, 0, c.F, c.B, fc, fh);
-        k_neighbor_stats<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, 1, c.F, c.B, bc, bh);
+        k_neighbor_stats<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, 0, c.F, c.B, fc, fh, cand);
+        k_neighbor_stats<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, 1, c.F, c.B, bc, bh, cand);
     } else {
-        k_neighbor_stats<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, 0, c.F, c.B, fc, fh);
-        k_neighbor_stats<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, 1, c.F, c.B, bc, bh);
+        k_neighbor_stats<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, 0, c.F, c.B, fc, fh, cand);
+        k_neighbor_stats<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, 1, c.F, c.B, bc, bh, cand);
     }
 }
 

@@ -163,6 +163,30 @@ class Solver:
                 _native.C.c_void_p(_stream_handle(dev))), "tsph_neighbor_stats")
         return fc[:nf], fh[:nf], bc[:nb], bh[:nb]
 
+    def candidate_stats(self):
+        """Per-particle number of candidates the density sweep's scan visits in
+        the fluid and the boundary grid, as int32 tensors [n_f, 2] and [n_b, 2]."""
+        nf, nb = self.fluid.part_num[None], self.bound.part_num[None]
+        dev = self.device
+        fc = torch.zeros((max(nf, 1), 2), dtype=torch.int32, device=dev)
+        bc = torch.zeros((max(nb, 1), 2), dtype=torch.int32, device=dev)
+        f, b = self._sets()
+        with torch.cuda.device(dev):
+            check(self._lib.tsph_candidate_stats(
+                self.ctx, f, b, _native.C.cast(fc.data_ptr(), _native._ip), _native.C.cast(bc.data_ptr(), _native._ip),
+                _native.C.c_void_p(_stream_handle(dev))), "tsph_candidate_stats")
+        return fc[:nf], bc[:nb]
+
+
+def fp32_fma_peak(device=None):
+    """FP32 FMA rate of the GPU in TFLOP/s (independent FMA chains on every SM)."""
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    out = _native.C.c_double(0.0)
+    with torch.cuda.device(dev):
+        check(_native.lib().tsph_fp32_fma_peak(_native.C.byref(out), _native.C.c_void_p(_stream_handle(dev))),
+              "tsph_fp32_fma_peak")
+    return float(out.value)
+
 
 def map_velocity(solver, grid):
     """Module-level form of ``map_velocity(ngrid, grid, fluid)`` (sph.py:382-397)."""
