@@ -515,6 +515,9 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
         e = cudaStreamCreateWithFlags(&box->x.cap_stream, cudaStreamNonBlocking);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&box->x.body_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         int rc = fail_cuda(e, "tsph_create");
@@ -590,6 +593,9 @@ int tsph_destroy(tsph_ctx *c) {
     for (void *p : box->x.pinned) cudaFreeHost(p);
     if (box->x.cap_stream) cudaStreamDestroy(box->x.cap_stream);
     if (box->x.body_stream) cudaStreamDestroy(box->x.body_stream);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete box;
     return TSPH_OK;
 }

@@ -28,6 +28,9 @@ struct tsph_ctx {
     int launches;             // kernel launches enqueued (counted by the launchers)
     int launches_per_step;    // top-level kernels of the last enqueued step
     int tpp;                  // threads per particle of the list sweeps (1, 2, 4, 8)
+    // second stream for the boundary set's share of a phase (fork_side / join_side)
+    cudaStream_t side;
+    cudaEvent_t ev_fork, ev_join;
 };
 
 namespace tsph {
@@ -35,6 +38,10 @@ namespace tsph {
 enum SolveKind { kSolveDiv = 0, kSolveDens = 1 };
 
 // grid.cu
+// fork_side: the side stream waits for `st`; join_side: `st` waits for the side
+// stream.  Inside a stream capture the pair becomes two branches of the graph.
+void fork_side(tsph_ctx &c, cudaStream_t st);
+void join_side(tsph_ctx &c, cudaStream_t st);
 void launch_step_begin(tsph_ctx &c, cudaStream_t st);
 void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st);
 void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);

@@ -536,6 +536,18 @@ __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, 
 }
 
 // ----------------------------------------------------------------------------- launchers
+void fork_side(tsph_ctx &c, cudaStream_t st) {
+    if (!c.side) return;
+    cudaEventRecord(c.ev_fork, st);
+    cudaStreamWaitEvent(c.side, c.ev_fork, 0);
+}
+
+void join_side(tsph_ctx &c, cudaStream_t st) {
+    if (!c.side) return;
+    cudaEventRecord(c.ev_join, c.side);
+    cudaStreamWaitEvent(st, c.ev_join, 0);
+}
+
 void launch_step_begin(tsph_ctx &c, cudaStream_t st) {
     cudaMemsetAsync(c.k.ss, 0, sizeof(SceneStep) * c.k.n_scenes, st);
     cudaMemsetAsync(c.k.dg, 0, sizeof(DevGlobal), st);
@@ -552,19 +564,24 @@ void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st) {
 
 void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st) {
     const int64_t nn = c.k.total_nodes;
-    cudaMemsetAsync(c.F.count, 0, sizeof(int) * nn, st);
-    cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, st);
     const int S = c.k.n_scenes;
     const int sb = (S + 127) / 128;
+    // the boundary set's encode, scatter and gather run on the side stream,
+    // beside the fluid's; the scans and sorts cover both grids in one launch
+    cudaStream_t sd = c.side ? c.side : st;
     c.launches += (f.n > 0) + (b.n > 0) + 3 + 1 + (f.n > 0) + (b.n > 0) + 2 + 2;
+    fork_side(c, st);
+    cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, sd);
+    if (b.n > 0) {
+        if (c.k.dim == 3) k_encode<3><<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, b, 1, c.B.count, c.B.slot);
+        else k_encode<2><<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, b, 1, c.B.count, c.B.slot);
+    }
+    cudaMemsetAsync(c.F.count, 0, sizeof(int) * nn, st);
     if (f.n > 0) {
         if (c.k.dim == 3) k_encode<3><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, 0, c.F.count, c.F.slot);
         else k_encode<2><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, 0, c.F.count, c.F.slot);
     }
-    if (b.n > 0) {
-        if (c.k.dim == 3) k_encode<3><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, 1, c.B.count, c.B.slot);
-        else k_encode<2><<<blocks_for(b.n), kBlock, 0, st>>>(c.k, b, 1, c.B.count, c.B.slot);
-    }
+    join_side(c, st);
     ScanArgs sa;
     sa.count[0] = c.F.count; sa.count[1] = c.B.count;
     sa.start[0] = c.F.start; sa.start[1] = c.B.start;
@@ -575,17 +592,21 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     k_scan_blocks<<<dim3(1, 2), kScanThreads, 0, st>>>(sa, nblk);
     k_scan_add<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk);
     k_scene_shift<<<sb, 128, 0, st>>>(c.k, c.F.start, c.B.start);
+    fork_side(c, st);
+    if (b.n > 0) k_scatter<<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm);
     if (f.n > 0) k_scatter<<<blocks_for(f.n), kBlock, 0, st>>>(c.k, 0, f.n, f.neighb_cell_seq, c.F.slot, c.F.start, c.F.perm);
-    if (b.n > 0) k_scatter<<<blocks_for(b.n), kBlock, 0, st>>>(c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm);
+    join_side(c, st);
     k_cell_sort<<<dim3(blocks_for(nn), 2), kBlock, 0, st>>>(c.k, c.F.start, c.F.perm, c.B.start, c.B.perm);
     k_tail_sort<<<sb, 128, 0, st>>>(c.k, c.F.perm, c.B.perm);
+    fork_side(c, st);
     if (c.k.dim == 3) {
+        k_gather_bound<3><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, b, c.B);
         k_gather_fluid<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F);
-        k_gather_bound<3><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, b, c.B);
     } else {
+        k_gather_bound<2><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, b, c.B);
         k_gather_fluid<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F);
-        k_gather_bound<2><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, b, c.B);
     }
+    join_side(c, st);
 }
 
 void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st) {
@@ -594,13 +615,16 @@ void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream
     // boundary: over the caller's count (the kernel returns past it); one block at least
     const int nbb = b.n > 0 ? blocks_for(b.n) : 1;
     c.launches += 2;
+    cudaStream_t sd = c.side ? c.side : st;
+    fork_side(c, st);
     if (c.k.dim == 3) {
+        k_update_bound<3><<<nbb, kBlock, 0, sd>>>(c.k, b, c.B, c.F.start);
         k_update_fluid<3><<<(int)c.k.f_ublocks, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
-        k_update_bound<3><<<nbb, kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
     } else {
+        k_update_bound<2><<<nbb, kBlock, 0, sd>>>(c.k, b, c.B, c.F.start);
         k_update_fluid<2><<<(int)c.k.f_ublocks, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
-        k_update_bound<2><<<nbb, kBlock, 0, st>>>(c.k, b, c.B, c.F.start);
     }
+    join_side(c, st);
 }
 
 void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, uint64_t *bh, int cand,

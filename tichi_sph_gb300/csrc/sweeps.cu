@@ -629,16 +629,21 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
     if (MULTI) { constexpr bool M = true; __VA_ARGS__; }                   \
     else { constexpr bool M = false; __VA_ARGS__; }
 
+// The boundary particles' own sums run on the side stream beside the fluid
+// sweep: neither writes what the other reads.
 void launch_density(tsph_ctx &c, cudaStream_t st) {
     c.launches += 2;
+    cudaStream_t sd = c.side ? c.side : st;
+    fork_side(c, st);
     TSPH_M_DISPATCH(c.n_scenes > 1,
         if (c.k.dim == 3) {
+            k_density_bound<3, M><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, c.F, c.B);
             k_density_fluid<3, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
-            k_density_bound<3, M><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
         } else {
+            k_density_bound<2, M><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, c.F, c.B);
             k_density_fluid<2, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
-            k_density_bound<2, M><<<blocks_for(c.B.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
         })
+    join_side(c, st);
 }
 
 void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
