@@ -158,8 +158,7 @@ int fbm_loop(tsph_ctx &c, cudaStream_t st, bool graph) {
 int enqueue_step(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st, bool with_cfl, bool graph) {
     c.launches = 0;
     launch_step_begin(c, st);
-    if (with_cfl) launch_cfl(c, f, st);
-    launch_grid_build(c, f, b, st);
+    launch_grid_build(c, f, b, st, with_cfl);
     launch_density(c, st);
     if (c.rec_tape) launch_tape_state(c, st);
     int rc = solve(c, kSolveDiv, st, graph);

@@ -44,7 +44,8 @@ void fork_side(tsph_ctx &c, cudaStream_t st);
 void join_side(tsph_ctx &c, cudaStream_t st);
 void launch_step_begin(tsph_ctx &c, cudaStream_t st);
 void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st);
-void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);
+// with_cfl: cfl_condition runs first on the side stream, beside the fluid's encode
+void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st, bool with_cfl = false);
 void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st);
 void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, uint64_t *bh, int cand,
                            cudaStream_t st);

@@ -562,7 +562,7 @@ void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st) {
     else k_cfl<2><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n);
 }
 
-void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st) {
+void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st, bool with_cfl) {
     const int64_t nn = c.k.total_nodes;
     const int S = c.k.n_scenes;
     const int sb = (S + 127) / 128;
@@ -571,6 +571,7 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     cudaStream_t sd = c.side ? c.side : st;
     c.launches += (f.n > 0) + (b.n > 0) + 3 + 1 + (f.n > 0) + (b.n > 0) + 2 + 2;
     fork_side(c, st);
+    if (with_cfl) launch_cfl(c, f, sd);  // nothing before the first solve reads dt
     cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, sd);
     if (b.n > 0) {
         if (c.k.dim == 3) k_encode<3><<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, b, 1, c.B.count, c.B.slot);
