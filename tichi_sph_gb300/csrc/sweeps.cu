@@ -195,7 +195,11 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
     F.comp[s] = comp;
     F.a1[s] = make_float4(a1x, a1y, a1z, 0.f);
     F.a2[s] = a2;
-    F.mpsi[s] = make_float4(mp.x, k.vfsph ? comp : rho, mp.z, alpha);
+    const float psi = k.vfsph ? comp : rho;
+    F.mpsi[s] = make_float4(mp.x, psi, mp.z, alpha);
+    // psi also rides in the current v_adv's unused w (the velocity sweeps carry
+    // it along), so the advection sweep gets it with the neighbour's v_adv
+    F.vadv[(int64_t)st.cur * F.cap + s].w = psi;
 }
 
 // The boundary's own sums: SPH_prepare_attr (b,b)(b,f), SPH_prepare_alpha_2 (b,f),
@@ -437,7 +441,7 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
             float4 *vout = F.vadv + (1 - cur) * F.cap;
             const float sc_ = -(1.f / k.sp[sc].dt) / F.mpsi[s].x;
             const float4 vi = vin[s];
-            vout[s] = make_float4(vi.x + sc_ * ax, vi.y + sc_ * ay, vi.z + sc_ * az, 0.f);
+            vout[s] = make_float4(vi.x + sc_ * ax, vi.y + sc_ * ay, vi.z + sc_ * az, vi.w);  // w: psi
         }
     }
     if (!block_last_warp(&arrived)) return;
@@ -587,7 +591,7 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                     }
                     const float4 pj = F.pos[j];
                     const float4 vj = vin[j];
-                    const float psij = F.mpsi[j].y;
+                    const float psij = vj.w;  // the neighbour's psi, set by the density sweep
                     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                     const float r2 = dx * dx + dy * dy + dz * dz;
                     float r;
