@@ -87,7 +87,7 @@ struct DevGlobal {
     int32_t pad;
 };
 
-enum GlobalTicket { kGtCfl = 0, kGtVel = 1, kGtFbm = 2, kGtUpdate = 3 };
+enum GlobalTicket { kGtCfl = 0, kGtVel = 1, kGtFbm = 2, kGtUpdate = 3, kGtScanF = 4, kGtScanB = 5, kGtScanDone = 6 };
 enum SceneTicket { kStPsi = 0, kStVel = 1, kStFbm = 2, kStUpdate = 3 };
 
 // Launch-time constants of one context (passed by value: the constant bank).

@@ -103,9 +103,13 @@ __global__ void __launch_bounds__(kBlock) k_encode(KConst k, tsph_set U, int bou
 }
 
 // ----------------------------------------------------------------------------- scan
-// Exclusive scan of the cell counts: 4096 cells per block, then a single-block
-// scan of the block totals, then the add.  blockIdx.y selects the fluid (0) or
-// boundary (1) grid.
+// Exclusive scan of the cell counts in two launches (blockIdx.y selects the
+// fluid (0) or boundary (1) grid; 4096 cells per block):
+//   k_scan_reduce: each block's total; the grid's last block to finish scans
+//     the totals in place (a ticket, no block waits for another);
+//   k_scan_down: each block scans its cells again and adds its offset; the last
+//     block over both grids derives the per-scene shifts from the finished
+//     starts.
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -145,7 +149,45 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total) {
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_local(ScanArgs a) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(ScanArgs a, int nblocks, unsigned int *tickets) {
+    __shared__ int sh[33];
+    const int g = blockIdx.y;
+    const int64_t base = blockIdx.x * (int64_t)kScanTile + threadIdx.x * kScanItems;
+    int sum = 0;
+#pragma unroll
+    for (int t = 0; t < kScanItems; ++t)
+        if (base + t < a.n) sum += a.count[g][base + t];
+    int total;
+    block_excl_scan(sum, sh, total);
+    if (threadIdx.x == 0) a.blocks[g][blockIdx.x] = total;
+    if (!last_block_done(&tickets[g], (unsigned int)nblocks)) return;
+    // this grid's block totals -> exclusive offsets, in place; [nblocks] = total
+    int carry = 0;
+    for (int b0 = 0; b0 < nblocks; b0 += kScanTile) {
+        int v[kScanItems];
+        int s = 0;
+        const int i0 = b0 + threadIdx.x * kScanItems;
+#pragma unroll
+        for (int t = 0; t < kScanItems; ++t) {
+            v[t] = (i0 + t < nblocks) ? __ldcg(&a.blocks[g][i0 + t]) : 0;
+            s += v[t];
+        }
+        int tot;
+        int run = block_excl_scan(s, sh, tot) + carry;
+#pragma unroll
+        for (int t = 0; t < kScanItems; ++t) {
+            if (i0 + t < nblocks) a.blocks[g][i0 + t] = run;
+            run += v[t];
+        }
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        a.blocks[g][nblocks] = carry;
+        tickets[g] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(ScanArgs a, int nblocks, KConst k, unsigned int *ticket) {
     __shared__ int sh[33];
     const int g = blockIdx.y;
     const int64_t base = blockIdx.x * (int64_t)kScanTile + threadIdx.x * kScanItems;
@@ -157,62 +199,27 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_local(ScanArgs a) {
         sum += v[t];
     }
     int total;
-    int run = block_excl_scan(sum, sh, total);
+    int run = block_excl_scan(sum, sh, total) + a.blocks[g][blockIdx.x];
 #pragma unroll
     for (int t = 0; t < kScanItems; ++t) {
         if (base + t < a.n) a.start[g][base + t] = run;
         run += v[t];
     }
-    if (threadIdx.x == 0) a.blocks[g][blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_blocks(ScanArgs a, int nblocks) {
-    __shared__ int sh[33];
-    const int g = blockIdx.y;
-    int carry = 0;
-    for (int base = 0; base < nblocks; base += kScanTile) {
-        int v[kScanItems];
-        int sum = 0;
-        const int i0 = base + threadIdx.x * kScanItems;
-#pragma unroll
-        for (int t = 0; t < kScanItems; ++t) {
-            v[t] = (i0 + t < nblocks) ? a.blocks[g][i0 + t] : 0;
-            sum += v[t];
-        }
-        int total;
-        int run = block_excl_scan(sum, sh, total) + carry;
-#pragma unroll
-        for (int t = 0; t < kScanItems; ++t) {
-            if (i0 + t < nblocks) a.blocks[g][i0 + t] = run;
-            run += v[t];
-        }
-        carry += total;
-    }
-    if (threadIdx.x == 0) a.blocks[g][nblocks] = carry;
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_add(ScanArgs a, int nblocks) {
-    const int g = blockIdx.y;
-    const int add = a.blocks[g][blockIdx.x];
-    const int64_t base = blockIdx.x * (int64_t)kScanTile;
-    for (int t = threadIdx.x; t < kScanTile; t += kScanThreads)
-        if (base + t < a.n) a.start[g][base + t] += add;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.start[g][a.n] = a.blocks[g][nblocks];
-}
-
-// Per scene: in-grid counts and the shift from global scan positions to the
-// scene's sorted slots.
-__global__ void k_scene_shift(KConst k, const int *__restrict__ fstart, const int *__restrict__ bstart) {
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < k.n_scenes; s += gridDim.x * blockDim.x) {
+    if (!last_block_done(ticket, 2u * (unsigned int)nblocks)) return;
+    // per scene: in-grid counts and the shift from global scan positions to the
+    // scene's sorted slots
+    for (int s = threadIdx.x; s < k.n_scenes; s += blockDim.x) {
         const SceneConst &c = k.sc[s];
         SceneStep &st = k.ss[s];
-        const int f0 = fstart[c.cbase], f1 = fstart[c.cbase + c.node_num];
-        const int b0 = bstart[c.cbase], b1 = bstart[c.cbase + c.node_num];
+        const int f0 = __ldcg(&a.start[0][c.cbase]), f1 = __ldcg(&a.start[0][c.cbase + c.node_num]);
+        const int b0 = __ldcg(&a.start[1][c.cbase]), b1 = __ldcg(&a.start[1][c.cbase + c.node_num]);
         st.f_in = f1 - f0;
         st.b_in = b1 - b0;
         st.f_shift = c.f_slot - f0;
         st.b_shift = c.b_slot - b0;
     }
+    if (threadIdx.x == 0) *ticket = 0;
 }
 
 // ----------------------------------------------------------------------------- scatter
@@ -569,7 +576,7 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     // the boundary set's encode, scatter and gather run on the side stream,
     // beside the fluid's; the scans and sorts cover both grids in one launch
     cudaStream_t sd = c.side ? c.side : st;
-    c.launches += (f.n > 0) + (b.n > 0) + 3 + 1 + (f.n > 0) + (b.n > 0) + 2 + 2;
+    c.launches += (f.n > 0) + (b.n > 0) + 2 + (f.n > 0) + (b.n > 0) + 2 + 2;
     fork_side(c, st);
     if (with_cfl) launch_cfl(c, f, sd);  // nothing before the first solve reads dt
     cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, sd);
@@ -589,10 +596,8 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     sa.blocks[0] = c.S.scan_blocks; sa.blocks[1] = c.S.scan_blocks + c.S.scan_len / 2;
     sa.n = nn;
     const int nblk = (int)((nn + kScanTile - 1) / kScanTile);
-    k_scan_local<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa);
-    k_scan_blocks<<<dim3(1, 2), kScanThreads, 0, st>>>(sa, nblk);
-    k_scan_add<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk);
-    k_scene_shift<<<sb, 128, 0, st>>>(c.k, c.F.start, c.B.start);
+    k_scan_reduce<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk, c.k.dg->ticket + kGtScanF);
+    k_scan_down<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk, c.k, c.k.dg->ticket + kGtScanDone);
     fork_side(c, st);
     if (b.n > 0) k_scatter<<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm);
     if (f.n > 0) k_scatter<<<blocks_for(f.n), kBlock, 0, st>>>(c.k, 0, f.n, f.neighb_cell_seq, c.F.slot, c.F.start, c.F.perm);
