@@ -257,11 +257,21 @@ __device__ __forceinline__ void insertion_sort(int *p, long long beg, long long 
 // network orders them, one write-back; larger cells use insertion_sort.
 constexpr int kRegSort = 16;
 
+// Threads past the last cell sort the scenes' tails of particles without a
+// valid cell, by id (one thread per scene and grid).
 __global__ void __launch_bounds__(kBlock) k_cell_sort(KConst k, const int *__restrict__ fstart, int *fperm,
                                                       const int *__restrict__ bstart, int *bperm) {
     const int g = blockIdx.y;
     const long long c = blockIdx.x * (long long)kBlock + threadIdx.x;
-    if (c >= k.total_nodes) return;
+    if (c >= k.total_nodes) {
+        const long long s = c - k.total_nodes;
+        if (s >= k.n_scenes) return;
+        const SceneConst &sc = k.sc[s];
+        const SceneStep &st = k.ss[s];
+        if (g == 0 && st.f_tail > 1) insertion_sort(fperm, sc.f_slot + st.f_in, sc.f_slot + st.f_in + st.f_tail);
+        if (g == 1 && st.b_tail > 1) insertion_sort(bperm, sc.b_slot + st.b_in, sc.b_slot + st.b_in + st.b_tail);
+        return;
+    }
     const int *start = g ? bstart : fstart;
     const int beg = start[c], end = start[c + 1];
     const int n = end - beg;
@@ -288,16 +298,6 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(KConst k, const int *__res
 #pragma unroll
     for (int i = 0; i < kRegSort; ++i)
         if (i < n) p[i] = v[i];
-}
-
-// Each scene's particles without a valid cell, ordered by id (one thread per scene).
-__global__ void k_tail_sort(KConst k, int *fperm, int *bperm) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= k.n_scenes) return;
-    const SceneConst &c = k.sc[s];
-    const SceneStep &st = k.ss[s];
-    if (st.f_tail > 1) insertion_sort(fperm, c.f_slot + st.f_in, c.f_slot + st.f_in + st.f_tail);
-    if (st.b_tail > 1) insertion_sort(bperm, c.b_slot + st.b_in, c.b_slot + st.b_in + st.b_tail);
 }
 
 // ----------------------------------------------------------------------------- gather
@@ -572,11 +572,10 @@ void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st) {
 void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st, bool with_cfl) {
     const int64_t nn = c.k.total_nodes;
     const int S = c.k.n_scenes;
-    const int sb = (S + 127) / 128;
     // the boundary set's encode, scatter and gather run on the side stream,
     // beside the fluid's; the scans and sorts cover both grids in one launch
     cudaStream_t sd = c.side ? c.side : st;
-    c.launches += (f.n > 0) + (b.n > 0) + 2 + (f.n > 0) + (b.n > 0) + 2 + 2;
+    c.launches += (f.n > 0) + (b.n > 0) + 2 + (f.n > 0) + (b.n > 0) + 1 + 2;
     fork_side(c, st);
     if (with_cfl) launch_cfl(c, f, sd);  // nothing before the first solve reads dt
     cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, sd);
@@ -602,8 +601,7 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     if (b.n > 0) k_scatter<<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm);
     if (f.n > 0) k_scatter<<<blocks_for(f.n), kBlock, 0, st>>>(c.k, 0, f.n, f.neighb_cell_seq, c.F.slot, c.F.start, c.F.perm);
     join_side(c, st);
-    k_cell_sort<<<dim3(blocks_for(nn), 2), kBlock, 0, st>>>(c.k, c.F.start, c.F.perm, c.B.start, c.B.perm);
-    k_tail_sort<<<sb, 128, 0, st>>>(c.k, c.F.perm, c.B.perm);
+    k_cell_sort<<<dim3(blocks_for(nn + S), 2), kBlock, 0, st>>>(c.k, c.F.start, c.F.perm, c.B.start, c.B.perm);
     fork_side(c, st);
     if (c.k.dim == 3) {
         k_gather_bound<3><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, b, c.B);
