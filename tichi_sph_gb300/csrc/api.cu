@@ -667,6 +667,8 @@ int tsph_profile_phases(tsph_ctx *c, const tsph_set *f, const tsph_set *b, int r
         launch_density(*c, st);
         launch_solve_begin(*c, kSolveDiv, 0, 0, st);
         launch_psi(*c, st);
+        // the density sweep did the first psi iteration's work: time full sweeps
+        if (ph == TSPH_PH_PSI) launch_clear_psi_ready(*c, st);
         TSPH_CK(cudaEventRecord(e0, st));
         for (int r = 0; r < reps; ++r) {
             switch (ph) {

@@ -75,6 +75,9 @@ struct SceneStep {
     int32_t status;
     int32_t f_tail, b_tail;     // particles without a valid cell
     int32_t f_in, b_in;         // particles in the grid
+    // 1 while psi_adv, kappa and psi_sum of the divergence solve's first
+    // iteration come from the density sweep (its psi sweep then does nothing)
+    int32_t psi_ready, pad0;
     long long f_shift, b_shift; // sorted slot of global scan position p is p + shift
     unsigned int ticket[6];     // block tickets of this scene (psi, vel, fbm, update)
     double psi_sum, kinetic_energy, potential_energy;

@@ -52,6 +52,7 @@ void launch_neighbor_stats(tsph_ctx &c, int32_t *fc, uint64_t *fh, int32_t *bc, 
 
 // sweeps.cu
 void launch_density(tsph_ctx &c, cudaStream_t st);
+void launch_clear_psi_ready(tsph_ctx &c, cudaStream_t st);
 void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
 void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
 void launch_psi(tsph_ctx &c, cudaStream_t st);

@@ -115,91 +115,157 @@ __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf 
     }
 }
 
+// In the one-scene instance the divergence solve's first psi sweep (k_psi's
+// work for its iteration 0) is done here as well when that solve will run
+// (iter_min > 0 or the carried-over compression above the tolerance, the test
+// k_solve_begin makes): its pair terms need only positions and the v_adv the
+// solve starts from, both fixed here, and walk the same pairs in the same
+// order as k_psi with one thread per particle, with the same arithmetic; the
+// scene's psi_sum goes through the same partials and ticket.  psi_ready tells
+// k_psi to skip that iteration.  (Measured: a saving in the one-scene case;
+// in the batched instance, whose scene lookups leave fewer registers, a loss.)
 template <int DIM, bool M>
-__global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf F, BoundBuf B) {
+__global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf F, BoundBuf B, double *partials) {
+    __shared__ double sh[kBlock / 32];
+    __shared__ unsigned int arrived;
+    if (threadIdx.x == 0) arrived = 0;
+    __syncthreads();
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int sc = f_block_scene<M>(k, blockIdx.x * (int64_t)kBlock);
     const SceneConst &c = scene<M>(k, sc);
-    if (s - c.f_slot >= c.f_n) return;
-    const SceneStep &st = k.ss[sc];
-    Geo g;
-    g.load(c, k.R);
-    const long long f_shift = shift_of<M>(st.f_shift), b_shift = shift_of<M>(st.b_shift);
-    const float4 pi = F.pos[s];
-    bool ok;
-    const long long code = cell_code<DIM>(pi, g, ok);
-    float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f;
-    float a1x = 0.f, a1y = 0.f, a1z = 0.f;
-    int nfl = 0, nbo = 0;
-    int *L = F.nbr;
-    const int64_t stride = F.cap;
-    const int cap = k.nbr_max;
-    const float w0 = kw(0.f) * g.sig;
-    if (ok) {
-        // phase 1: record the pairs
-        visit_candidates_within<DIM>(F.start, g, pi, code, f_shift, 0, [&](int j) {
-            const float4 pj = F.pos[j];
+    SceneStep &st = k.ss[sc];
+    const bool psi0 = !M && c.f_n > 0 && ((0 < c.iter_min) || (k.sp[sc].compression > (double)c.div_tol));
+    double contrib = 0.0;
+    if (s - c.f_slot < c.f_n) {
+        Geo g;
+        g.load(c, k.R);
+        const long long f_shift = shift_of<M>(st.f_shift), b_shift = shift_of<M>(st.b_shift);
+        const float4 pi = F.pos[s];
+        const float4 *vin = F.vadv + st.cur * F.cap;
+        const float4 vi = psi0 ? vin[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+        bool ok;
+        const long long code = cell_code<DIM>(pi, g, ok);
+        float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f, pacc = 0.f;
+        float a1x = 0.f, a1y = 0.f, a1z = 0.f;
+        int nfl = 0, nbo = 0;
+        int *L = F.nbr;
+        const int64_t stride = F.cap;
+        const int cap = k.nbr_max;
+        const float w0 = kw(0.f) * g.sig;
+        // k_psi's pair term (IPPE_adv_psi), the same expression
+        auto psi_pair = [&](const float4 *P, const float4 *V, int j, auto listed) {
+            constexpr bool Ls = decltype(listed)::value;
+            const float4 pj = P[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < g.h2) {
-                if (r2 > 0.f) {
-                    if (nfl < cap) L[nbr_index(nfl, s, stride)] = j;
-                    ++nfl;
-                } else {
-                    const float2 mv = F.mv[j];
-                    wsum += w0;
-                    rho += w0 * mv.x;
-                    comp += w0 * mv.y;
-                }
+            if (Ls || (r2 < g.h2 && r2 > 0.f)) {
+                const float4 vj = V[j];
+                float r;
+                const float ri = Ls ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
+                const float f = kwg(r * g.inv_h) * g.sig_h * ri * pj.w;
+                pacc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
             }
-        });
-        visit_candidates_within<DIM>(B.start, g, pi, code, b_shift, 0, [&](int j) {
-            const float4 pj = B.pos[j];
-            const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < g.h2) {
-                if (r2 > 0.f) {
-                    const int t = nfl + nbo;
-                    if (t < cap) L[nbr_index(t, s, stride)] = j;
-                    ++nbo;
-                } else {
-                    const float2 mv = B.mv[j];
-                    wsum += w0;
-                    rho += w0 * mv.x;
-                    comp += w0 * mv.y;
+        };
+        if (ok) {
+            // phase 1: record the pairs
+            visit_candidates_within<DIM>(F.start, g, pi, code, f_shift, 0, [&](int j) {
+                const float4 pj = F.pos[j];
+                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 < g.h2) {
+                    if (r2 > 0.f) {
+                        if (nfl < cap) L[nbr_index(nfl, s, stride)] = j;
+                        ++nfl;
+                    } else {
+                        const float2 mv = F.mv[j];
+                        wsum += w0;
+                        rho += w0 * mv.x;
+                        comp += w0 * mv.y;
+                    }
                 }
+            });
+            visit_candidates_within<DIM>(B.start, g, pi, code, b_shift, 0, [&](int j) {
+                const float4 pj = B.pos[j];
+                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 < g.h2) {
+                    if (r2 > 0.f) {
+                        const int t = nfl + nbo;
+                        if (t < cap) L[nbr_index(t, s, stride)] = j;
+                        ++nbo;
+                    } else {
+                        const float2 mv = B.mv[j];
+                        wsum += w0;
+                        rho += w0 * mv.x;
+                        comp += w0 * mv.y;
+                    }
+                }
+            });
+            if (nfl + nbo <= cap) {
+                // phase 2: the arithmetic over the recorded pairs
+                walk_blocks<1>(F.nbr, s, stride, 0, nfl, nfl + nbo,
+                    [&](int j) {
+                        density_pair_fluid<DIM, true>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
+                        if (psi0) psi_pair(F.pos, vin, j, std::true_type{});
+                    },
+                    [&](int j) {
+                        density_pair_bound<DIM, true>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z);
+                        if (psi0) psi_pair(B.pos, B.vadv, j, std::true_type{});
+                    });
+            } else {
+                // list overflow: one scan with the arithmetic inline
+                wsum = rho = comp = a2 = a1x = a1y = a1z = 0.f;
+                visit_candidates<DIM>(F.start, g, code, f_shift, 0, [&](int j) {
+                    density_pair_fluid<DIM>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
+                    if (psi0) psi_pair(F.pos, vin, j, std::false_type{});
+                });
+                visit_candidates<DIM>(B.start, g, code, b_shift, 0, [&](int j) {
+                    density_pair_bound<DIM>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z);
+                    if (psi0) psi_pair(B.pos, B.vadv, j, std::false_type{});
+                });
             }
-        });
-        if (nfl + nbo <= cap) {
-            // phase 2: the arithmetic over the recorded pairs
-            walk_blocks<1>(F.nbr, s, stride, 0, nfl, nfl + nbo,
-                [&](int j) { density_pair_fluid<DIM, true>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2); },
-                [&](int j) { density_pair_bound<DIM, true>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z); });
-        } else {
-            // list overflow: one scan with the arithmetic inline
-            wsum = rho = comp = a2 = a1x = a1y = a1z = 0.f;
-            visit_candidates<DIM>(F.start, g, code, f_shift, 0, [&](int j) {
-                density_pair_fluid<DIM>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
-            });
-            visit_candidates<DIM>(B.start, g, code, b_shift, 0, [&](int j) {
-                density_pair_bound<DIM>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z);
-            });
+        }
+        F.nbr_cnt[s] = (nfl + nbo <= cap) ? ((unsigned int)nfl | ((unsigned int)nbo << 16)) : kNbrOverflow;
+        const float4 mp = F.mpsi[s];
+        float alpha = (a1x * a1x + a1y * a1y + a1z * a1z) / mp.x + a2;
+        if (alpha < 1e-4f) alpha = 1e-4f;
+        F.W[s] = wsum;
+        F.rho[s] = rho;
+        F.comp[s] = comp;
+        F.a1[s] = make_float4(a1x, a1y, a1z, 0.f);
+        F.a2[s] = a2;
+        const float psi = k.vfsph ? comp : rho;
+        F.mpsi[s] = make_float4(mp.x, psi, mp.z, alpha);
+        // psi also rides in the current v_adv's unused w (the velocity sweeps carry
+        // it along), so the advection sweep gets it with the neighbour's v_adv
+        F.vadv[(int64_t)st.cur * F.cap + s].w = psi;
+        if (psi0) {
+            // IPPE_adv_psi_init + IPPE_psi_adv_non_negative, as k_psi
+            float pa = (psi - mp.z) + pacc * k.sp[sc].dt;
+            if (pa < 0.f) pa = 0.f;
+            F.psiadv[s] = pa;
+            F.kappa[s] = pa / alpha;
+            contrib = (double)(pa / mp.z);
         }
     }
-    F.nbr_cnt[s] = (nfl + nbo <= cap) ? ((unsigned int)nfl | ((unsigned int)nbo << 16)) : kNbrOverflow;
-    const float4 mp = F.mpsi[s];
-    float alpha = (a1x * a1x + a1y * a1y + a1z * a1z) / mp.x + a2;
-    if (alpha < 1e-4f) alpha = 1e-4f;
-    F.W[s] = wsum;
-    F.rho[s] = rho;
-    F.comp[s] = comp;
-    F.a1[s] = make_float4(a1x, a1y, a1z, 0.f);
-    F.a2[s] = a2;
-    const float psi = k.vfsph ? comp : rho;
-    F.mpsi[s] = make_float4(mp.x, psi, mp.z, alpha);
-    // psi also rides in the current v_adv's unused w (the velocity sweeps carry
-    // it along), so the advection sweep gets it with the neighbour's v_adv
-    F.vadv[(int64_t)st.cur * F.cap + s].w = psi;
+    if (!psi0) return;  // uniform over the block (one scene)
+    double bsum;
+    if (block_sum_last_warp<kBlock>(contrib, sh, &arrived, bsum)) {
+        if ((threadIdx.x & 31) == 0) partials[blockIdx.x] = bsum;
+        const int64_t b0 = c.f_slot / kBlock;
+        const unsigned int nblk = (unsigned int)(c.f_slots / kBlock);
+        if (last_warp_done(&st.ticket[kStPsi], nblk)) {
+            const int lane = threadIdx.x & 31;
+            double v = 0.0;
+            for (int64_t i = lane; i < (int64_t)nblk; i += 32) v += __ldcg(partials + b0 + i);
+            v = warp_sum(v);
+            if (lane == 0) {
+                st.psi_sum = v;
+                st.ticket[kStPsi] = 0;
+                st.psi_ready = 1;
+            }
+        }
+    }
 }
 
 // The boundary's own sums: SPH_prepare_attr (b,b)(b,f), SPH_prepare_alpha_2 (b,f),
@@ -319,6 +385,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBu
     const int sc = f_block_scene<M>(k, first);
     SceneStep &st = k.ss[sc];
     if (!st.cond) return;  // this scene's loop has ended (uniform over the block)
+    if (st.psi_ready) return;  // this iteration's sweep ran inside the density sweep
     if (threadIdx.x == 0) arrived = 0;
     __syncthreads();
     const SceneConst &c = scene<M>(k, sc);
@@ -461,6 +528,7 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
             if (capped) st.status |= (kind == kSolveDiv ? TSPH_ST_DIV_ITER_CAP : TSPH_ST_DENS_ITER_CAP);
             st.cond = cond;
             st.cur = 1 - st.cur;
+            st.psi_ready = 0;
             st.ticket[kStVel] = 0;
         }
     }
@@ -642,13 +710,21 @@ void launch_density(tsph_ctx &c, cudaStream_t st) {
     TSPH_M_DISPATCH(c.n_scenes > 1,
         if (c.k.dim == 3) {
             k_density_bound<3, M><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, c.F, c.B);
-            k_density_fluid<3, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+            k_density_fluid<3, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
         } else {
             k_density_bound<2, M><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, c.F, c.B);
-            k_density_fluid<2, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+            k_density_fluid<2, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
         })
     join_side(c, st);
 }
+
+// Measurement only: lets the next psi sweep run in full although the density
+// sweep did its first iteration's work.
+__global__ void k_clear_psi_ready(KConst k) {
+    for (int s = threadIdx.x; s < k.n_scenes; s += blockDim.x) k.ss[s].psi_ready = 0;
+}
+
+void launch_clear_psi_ready(tsph_ctx &c, cudaStream_t st) { k_clear_psi_ready<<<1, 256, 0, st>>>(c.k); }
 
 void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
     c.launches += 1;
