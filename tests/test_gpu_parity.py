@@ -282,3 +282,61 @@ def test_bitwise_deterministic(scene):
     a, b = outs
     for x, y in zip(a, b):
         np.testing.assert_array_equal(np.asarray(x), np.asarray(y))
+
+
+def _make_gpu_cfg(cfg_d, scen_d, fluid_arrays, bound_arrays):
+    from tichi_sph_gb300 import sph_config, Fluid, Solver
+    cfg = sph_config.Config(cfg_d, scen_d)
+    objs = []
+    for uid, (cap, arrs) in enumerate(((cfg.fluid_max_part_num[None], fluid_arrays),
+                                       (cfg.bound_max_part_num[None], bound_arrays))):
+        o = Fluid(cap, cfg, uid, device="cuda")
+        n = len(arrs["pos"])
+        o.part_num[None] = n
+        for k, v in arrs.items():
+            getattr(o, k)[:n] = torch.as_tensor(np.asarray(v, dtype=np.float32), device="cuda").reshape(
+                getattr(o, k)[:n].shape)
+        objs.append(o)
+    return cfg, objs[0], objs[1], Solver(cfg, objs[0], objs[1])
+
+
+@pytest.mark.parametrize("iter_min,carried", [(0, 0.0), (0, 0.5), (1, 0.0)])
+def test_iteration_floor_and_carried_compression(iter_min, carried):
+    """solver_iter_threshold_min below 2 (the golden scenes all use 2): with 0
+    a solve runs only while the compression carried over from the previous
+    solve is above its tolerance (main.py:201), so its first iteration may or
+    may not run; with 1 the first runs and later ones follow the tolerance.
+    Three chained substeps of the dfsph3d scene, GPU vs oracle: identical
+    iteration counts, fields within 10x the one-step tolerance."""
+    _need_cuda()
+    import json
+    scene = "dfsph3d"
+    cpath, spath = G.paths(scene)
+    cfg_d, scen_d = json.load(open(cpath)), json.load(open(spath))
+    cfg_d["solver_iter_threshold_min"] = iter_min
+    init, _ = G.load(scene)
+    fa, ba = G.init_arrays(init, "fluid"), G.init_arrays(init, "bound")
+    cfg, fl, bd, solver = _make_gpu_cfg(cfg_d, scen_d, fa, ba)
+    p = O.Params.from_config(cfg_d, scen_d, taichi_f32=True)
+    f64 = lambda d: {k: np.asarray(v, dtype=np.float32).astype(np.float64) for k, v in d.items()}
+    ofl, obd = O.sets_from_arrays(p, f64(fa), f64(ba))
+    solver.set_state(time_count=0.0, compression=carried)
+    ofl.compression = carried
+    st = O.Stats()
+    iters = []
+    for step in range(3):
+        solver.substep()
+        gs = solver.stats()
+        O.run_substep(ofl, obd, p, st)
+        assert (gs["div_iter"], gs["incom_iter"]) == (st.div_iter, st.incom_iter), (step, gs, vars(st))
+        iters.append((st.div_iter, st.incom_iter))
+        dens = float(np.abs(ofl.sph_density).max(initial=0.0))
+        compare(scene, "floor%d step%d" % (iter_min, step), fl, ofl, _fluid_fields(scene, p), tol_scale=10.0,
+                dens_scale=dens)
+    solver.close()
+    if iter_min == 0 and carried == 0.0:
+        assert iters[0] == (0, 0)
+    if iter_min == 0 and carried > 0.0:
+        assert iters[0][0] >= 1
+    if iter_min == 1:
+        assert all(d >= 1 and i >= 1 for d, i in iters)
