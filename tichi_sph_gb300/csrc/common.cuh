@@ -485,19 +485,21 @@ struct Lanes {
 // neighbours (ff), nfl <= t < ntot boundary ones (fb).  The next block's int4 is
 // loaded before the current block is processed, and the four callbacks of a
 // block only accumulate into registers, so their gathers can all be in flight
-// together.
-template <int TPP, class FF, class FB>
+// together.  NC = false: the list was written by the calling kernel (plain
+// loads instead of the read-only path).
+template <int TPP, bool NC = true, class FF, class FB>
 __device__ __forceinline__ void walk_blocks(const int *__restrict__ nbr, int64_t s, int64_t cap, int q,
                                             int nfl, int ntot, FF &&ff, FB &&fb) {
     const int4 *L4 = reinterpret_cast<const int4 *>(nbr) + s;
     const int nblk = (ntot + 3) >> 2;
     int b = q;
     if (b >= nblk) return;
-    int4 cur = __ldg(L4 + (int64_t)b * cap);
+    auto ld = [&](int64_t i) { return NC ? __ldg(L4 + i) : L4[i]; };
+    int4 cur = ld((int64_t)b * cap);
     while (b < nblk) {
         const int bn = b + TPP;
         int4 nxt = cur;
-        if (bn < nblk) nxt = __ldg(L4 + (int64_t)bn * cap);
+        if (bn < nblk) nxt = ld((int64_t)bn * cap);
         const int t0 = b << 2;
         const int jj[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll

@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
             });
             if (nfl + nbo <= cap) {
                 // phase 2: the arithmetic over the recorded pairs
-                walk_blocks<1>(F.nbr, s, stride, 0, nfl, nfl + nbo,
+                walk_blocks<1, false>(F.nbr, s, stride, 0, nfl, nfl + nbo,
                     [&](int j) {
                         density_pair_fluid<DIM, true>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
                         if (psi0) psi_pair(F.pos, vin, j, std::true_type{});
