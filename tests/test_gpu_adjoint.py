@@ -84,7 +84,7 @@ def test_adjoint_matches_fp64_autograd_and_fd():
     Lr, xr = _ref_loss(sc, x0, v, m, target)
     Lr.backward()
     assert float((xT - xr.detach()).abs().max()) < 2e-6          # forward: FP32 vs FP64 trajectories
-    assert abs(L - float(Lr)) <= 1e-4 * abs(float(Lr))
+    assert abs(L - float(Lr.detach())) <= 1e-4 * abs(float(Lr.detach()))
     rel_v = float((gv - v.grad).norm() / v.grad.norm())
     rel_mu = abs(gmu - float(m.grad)) / abs(float(m.grad))
     assert rel_v < 1e-3, rel_v
