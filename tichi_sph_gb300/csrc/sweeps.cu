@@ -167,15 +167,26 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
             }
         };
         if (ok) {
-            // phase 1: record the pairs
+            // phase 1: record the pairs.  The write position walks the blocked
+            // layout (entry t at nbr_index(t, s, stride)): +1 within a block of
+            // four, +4 stride - 3 to the next block
+            int nrec = 0;
+            int *wp = L + (int64_t)s * 4;
+            const int64_t next_block = stride * 4 - 3;
+            auto record = [&](int j) {
+                if (nrec < cap) {
+                    *wp = j;
+                    wp += ((nrec & 3) == 3) ? next_block : 1;
+                }
+                ++nrec;
+            };
             visit_candidates_within<DIM>(F.start, g, pi, code, f_shift, 0, [&](int j) {
                 const float4 pj = F.pos[j];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < g.h2) {
                     if (r2 > 0.f) {
-                        if (nfl < cap) L[nbr_index(nfl, s, stride)] = j;
-                        ++nfl;
+                        record(j);
                     } else {
                         const float2 mv = F.mv[j];
                         wsum += w0;
@@ -184,15 +195,14 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
                     }
                 }
             });
+            nfl = nrec;
             visit_candidates_within<DIM>(B.start, g, pi, code, b_shift, 0, [&](int j) {
                 const float4 pj = B.pos[j];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < g.h2) {
                     if (r2 > 0.f) {
-                        const int t = nfl + nbo;
-                        if (t < cap) L[nbr_index(t, s, stride)] = j;
-                        ++nbo;
+                        record(j);
                     } else {
                         const float2 mv = B.mv[j];
                         wsum += w0;
@@ -201,6 +211,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
                     }
                 }
             });
+            nbo = nrec - nfl;
             if (nfl + nbo <= cap) {
                 // phase 2: the arithmetic over the recorded pairs
                 walk_blocks<1, false>(F.nbr, s, stride, 0, nfl, nfl + nbo,
