@@ -337,10 +337,10 @@ __device__ __forceinline__ void visit_candidates_lean(const int *__restrict__ st
 // of distance from lb, for the particle and for the candidate's own cell), so
 // the margin on h^2 grows with it too.  Without row_trim (a row could alias
 // another) the margin is infinite: every candidate is visited.
-template <int DIM, int TPP = 1, class F>
-__device__ __forceinline__ void visit_candidates_within(const int *__restrict__ start, const Geo &g, float4 p,
-                                                        long long code, long long shift, int q, F &&f) {
-    const int R = g.R;
+template <int DIM, int TPP, int RR, class F>
+__device__ __forceinline__ void visit_within_impl(const int *__restrict__ start, const Geo &g, float4 p,
+                                                  long long code, long long shift, int q, F &&f) {
+    const int R = RR ? RR : g.R;
     const int zr = (DIM == 3) ? R : 0;
     // distance of the particle to its cell's lower / upper faces in x, y and z
     const float qx = __fdiv_rn(p.x - g.lb[0], g.h);
@@ -348,8 +348,10 @@ __device__ __forceinline__ void visit_candidates_within(const int *__restrict__ 
     const float fx = qx - floorf(qx), fy = qy - floorf(qy), fz = qz - floorf(qz);
     const float qm = fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz))) + (float)(R + 1);
     const float skip2 = g.row_trim ? g.h2 * (1.f + 1e-5f + 2e-6f * (float)R * qm) : __int_as_float(0x7f800000);
+#pragma unroll 1
     for (int dz = -zr; dz <= zr; ++dz) {
         const float ez = dz == 0 ? 0.f : (dz < 0 ? fz + (float)(-dz - 1) : (1.f - fz) + (float)(dz - 1)) * g.h;
+#pragma unroll 1
         for (int dy = -R; dy <= R; ++dy) {
             const float ey = dy == 0 ? 0.f : (dy < 0 ? fy + (float)(-dy - 1) : (1.f - fy) + (float)(dy - 1)) * g.h;
             const float eyz = ey * ey + ez * ez;
@@ -357,11 +359,13 @@ __device__ __forceinline__ void visit_candidates_within(const int *__restrict__ 
             long long rc = code + dy * g.nx + dz * g.nxny;
             long long lo = rc - R, hi = rc + R;
             // the row's end cells that lie farther than h (in x together with y / z)
+#pragma unroll
             for (int dx = -R; dx < 0; ++dx) {
                 const float ex = (fx + (float)(-dx - 1)) * g.h;
                 if (eyz + ex * ex > skip2) lo = rc + dx + 1;
                 else break;
             }
+#pragma unroll
             for (int dx = R; dx > 0; --dx) {
                 const float ex = ((1.f - fx) + (float)(dx - 1)) * g.h;
                 if (eyz + ex * ex > skip2) hi = rc + dx - 1;
@@ -375,6 +379,15 @@ __device__ __forceinline__ void visit_candidates_within(const int *__restrict__ 
             for (int j = beg + q; j < end; j += TPP) f(j);
         }
     }
+}
+
+// The template radius r = 1 (the reference's configurations) with the end-cell
+// tests unrolled, any other radius read at run time; the same arithmetic.
+template <int DIM, int TPP = 1, class F>
+__device__ __forceinline__ void visit_candidates_within(const int *__restrict__ start, const Geo &g, float4 p,
+                                                        long long code, long long shift, int q, F &&f) {
+    if (g.R == 1) visit_within_impl<DIM, TPP, 1>(start, g, p, code, shift, q, f);
+    else visit_within_impl<DIM, TPP, 0>(start, g, p, code, shift, q, f);
 }
 
 // ---------------------------------------------------------------------------------
