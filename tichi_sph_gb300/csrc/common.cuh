@@ -337,10 +337,10 @@ __device__ __forceinline__ void visit_candidates_lean(const int *__restrict__ st
 // of distance from lb, for the particle and for the candidate's own cell), so
 // the margin on h^2 grows with it too.  Without row_trim (a row could alias
 // another) the margin is infinite: every candidate is visited.
-template <int DIM, int TPP, int RR, class F>
-__device__ __forceinline__ void visit_within_impl(const int *__restrict__ start, const Geo &g, float4 p,
-                                                  long long code, long long shift, int q, F &&f) {
-    const int R = RR ? RR : g.R;
+template <int DIM, int TPP, class F>
+__device__ __forceinline__ void visit_within_any(const int *__restrict__ start, const Geo &g, float4 p,
+                                                 long long code, long long shift, int q, F &&f) {
+    const int R = g.R;
     const int zr = (DIM == 3) ? R : 0;
     // distance of the particle to its cell's lower / upper faces in x, y and z
     const float qx = __fdiv_rn(p.x - g.lb[0], g.h);
@@ -348,10 +348,8 @@ __device__ __forceinline__ void visit_within_impl(const int *__restrict__ start,
     const float fx = qx - floorf(qx), fy = qy - floorf(qy), fz = qz - floorf(qz);
     const float qm = fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz))) + (float)(R + 1);
     const float skip2 = g.row_trim ? g.h2 * (1.f + 1e-5f + 2e-6f * (float)R * qm) : __int_as_float(0x7f800000);
-#pragma unroll 1
     for (int dz = -zr; dz <= zr; ++dz) {
         const float ez = dz == 0 ? 0.f : (dz < 0 ? fz + (float)(-dz - 1) : (1.f - fz) + (float)(dz - 1)) * g.h;
-#pragma unroll 1
         for (int dy = -R; dy <= R; ++dy) {
             const float ey = dy == 0 ? 0.f : (dy < 0 ? fy + (float)(-dy - 1) : (1.f - fy) + (float)(dy - 1)) * g.h;
             const float eyz = ey * ey + ez * ez;
@@ -359,13 +357,11 @@ __device__ __forceinline__ void visit_within_impl(const int *__restrict__ start,
             long long rc = code + dy * g.nx + dz * g.nxny;
             long long lo = rc - R, hi = rc + R;
             // the row's end cells that lie farther than h (in x together with y / z)
-#pragma unroll
             for (int dx = -R; dx < 0; ++dx) {
                 const float ex = (fx + (float)(-dx - 1)) * g.h;
                 if (eyz + ex * ex > skip2) lo = rc + dx + 1;
                 else break;
             }
-#pragma unroll
             for (int dx = R; dx > 0; --dx) {
                 const float ex = ((1.f - fx) + (float)(dx - 1)) * g.h;
                 if (eyz + ex * ex > skip2) hi = rc + dx - 1;
@@ -381,13 +377,49 @@ __device__ __forceinline__ void visit_within_impl(const int *__restrict__ start,
     }
 }
 
-// The template radius r = 1 (the reference's configurations) with the end-cell
-// tests unrolled, any other radius read at run time; the same arithmetic.
+// visit_within_any for the template radius 1: the face distances (fy h,
+// (1 - fy) h and their x and z counterparts; the general form adds an exact
+// 0.f) and the end-cell squares are computed once per particle, not per row.
+template <int DIM, int TPP, class F>
+__device__ __forceinline__ void visit_within_r1(const int *__restrict__ start, const Geo &g, float4 p,
+                                                long long code, long long shift, int q, F &&f) {
+    const int zr = (DIM == 3) ? 1 : 0;
+    const float qx = __fdiv_rn(p.x - g.lb[0], g.h);
+    const float qy = __fdiv_rn(p.y - g.lb[1], g.h), qz = DIM == 3 ? __fdiv_rn(p.z - g.lb[2], g.h) : 0.f;
+    const float fx = qx - floorf(qx), fy = qy - floorf(qy), fz = qz - floorf(qz);
+    const float qm = fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz))) + 2.f;
+    const float skip2 = g.row_trim ? g.h2 * (1.f + 1e-5f + 2e-6f * qm) : __int_as_float(0x7f800000);
+    const float eym = fy * g.h, eyp = (1.f - fy) * g.h, ezm = fz * g.h, ezp = (1.f - fz) * g.h;
+    const float exm = fx * g.h, exp_ = (1.f - fx) * g.h;
+#pragma unroll 1
+    for (int dz = -zr; dz <= zr; ++dz) {
+        const float ez = dz == 0 ? 0.f : (dz < 0 ? ezm : ezp);
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const float ey = dy == 0 ? 0.f : (dy < 0 ? eym : eyp);
+            const float eyz = ey * ey + ez * ez;
+            if (eyz > skip2) continue;
+            const long long rc = code + dy * g.nx + dz * g.nxny;
+            // the row's end cells that lie farther than h (in x together with y / z)
+            long long lo = (eyz + exm * exm > skip2) ? rc : rc - 1;
+            long long hi = (eyz + exp_ * exp_ > skip2) ? rc : rc + 1;
+            if (lo < 1) lo = 1;
+            if (hi > g.node_num - 1) hi = g.node_num - 1;
+            if (lo > hi) continue;
+            const int beg = (int)(__ldg(start + g.cbase + lo) + shift);
+            const int end = (int)(__ldg(start + g.cbase + hi + 1) + shift);
+            for (int j = beg + q; j < end; j += TPP) f(j);
+        }
+    }
+}
+
+// The template radius r = 1 (the reference's configurations) in its own form,
+// any other radius read at run time; the same candidates.
 template <int DIM, int TPP = 1, class F>
 __device__ __forceinline__ void visit_candidates_within(const int *__restrict__ start, const Geo &g, float4 p,
                                                         long long code, long long shift, int q, F &&f) {
-    if (g.R == 1) visit_within_impl<DIM, TPP, 1>(start, g, p, code, shift, q, f);
-    else visit_within_impl<DIM, TPP, 0>(start, g, p, code, shift, q, f);
+    if (g.R == 1) visit_within_r1<DIM, TPP>(start, g, p, code, shift, q, f);
+    else visit_within_any<DIM, TPP>(start, g, p, code, shift, q, f);
 }
 
 // ---------------------------------------------------------------------------------
