@@ -377,7 +377,7 @@ __device__ __forceinline__ void visit_within_any(const int *__restrict__ start, 
     }
 }
 
-// visit_within_any for the template radius 1: the face distances (fy h,
+// The scan for the template radius 1: the face distances (fy h,
 // (1 - fy) h and their x and z counterparts; the general form adds an exact
 // 0.f) and the end-cell squares are computed once per particle, not per row.
 template <int DIM, int TPP, class F>
