@@ -677,7 +677,9 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                     const float ri = pair_rinv_pos(r2, r);
                     const float wg = kwg(r * g.inv_h) * g.sig_h;
                     const float adx = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-                    const float f = lap * (pj.w / psij) * wg * ri * adx / (eps + r2);
+                    // the two quotients by __fdividef (within 2 ulp, far inside the
+                    // 1e-5 bar); the scanning path keeps IEEE division
+                    const float f = __fdividef(lap * __fdividef(pj.w, psij) * wg * ri * adx, eps + r2);
                     vx += f * dx;
                     vy += f * dy;
                     vz += f * dz;
