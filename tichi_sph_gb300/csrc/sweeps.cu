@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
                     if (!L) psij = F.mpsi[j].y;
                     float r;
                     const float ri = L ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
-                    const float f = -pj.w / psij * (kwg(r * g.inv_h) * g.sig_h) * ri;
+                    const float f = -__fdividef(pj.w, psij) * (kwg(r * g.inv_h) * g.sig_h) * ri;
                     nx += f * dx;
                     ny += f * dy;
                     nz += f * dz;
@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                 const float ri = pair_rinv(r2, r);
                 const float wg = kwg(r * g.inv_h) * g.sig_h;
                 const float adx = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-                const float f = lap * (pj.w / psij) * wg * ri * adx / (eps + r2);
+                const float f = __fdividef(lap * __fdividef(pj.w, psij) * wg * ri * adx, eps + r2);
                 vx += f * dx;
                 vy += f * dy;
                 vz += f * dz;
@@ -647,7 +647,7 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                     float r;
                     const float ri = pair_rinv(r2, r);
                     const float coh = -gamma * mpj.x * (kcoh(r * g.inv_h) * c_coh) * ri;
-                    const float fac = 2.f * mpi.z / (mpi.y + mpj.y);
+                    const float fac = __fdividef(2.f * mpi.z, mpi.y + mpj.y);
                     sx += fac * (coh * dx + gamma * (ni.x - nj.x));
                     sy += fac * (coh * dy + gamma * (ni.y - nj.y));
                     sz += fac * (coh * dz + gamma * (ni.z - nj.z));
@@ -678,7 +678,7 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                     const float wg = kwg(r * g.inv_h) * g.sig_h;
                     const float adx = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
                     // the two quotients by __fdividef (within 2 ulp, far inside the
-                    // 1e-5 bar); the scanning path keeps IEEE division
+                    // 1e-5 bar), as on every per-pair path of these sweeps
                     const float f = __fdividef(lap * __fdividef(pj.w, psij) * wg * ri * adx, eps + r2);
                     vx += f * dx;
                     vy += f * dy;
