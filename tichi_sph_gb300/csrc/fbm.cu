@@ -124,11 +124,14 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, Bound
                     if (!(r2 < g.h2 && r2 > 0.f)) return;
                     const int fj = F.flagpass[j];
                     if (fj != 0 && fj != pass) return;
-                    const float r = sqrtf(r2);
+                    // pair geometry from rsqrt and a fast quotient (as the other
+                    // sweeps; within a few ulp)
+                    float r;
+                    const float ri = pair_rinv_pos(r2, r);
                     const float wg = kwg(r * g.inv_h) * g.sig_h;
                     const float Vj = F.mv[j].y;
-                    const float gx = dx / r * wg, gy = dy / r * wg, gz = dz / r * wg;
-                    const float dif = cd * Vj * r * wg / (r2 + eps);
+                    const float gx = dx * ri * wg, gy = dy * ri * wg, gz = dz * ri * wg;
+                    const float dif = __fdividef(cd * Vj * r * wg, r2 + eps);
 #pragma unroll
                     for (int q = 0; q < P; ++q) {
                         const float vfj = F.vf[q * F.cap + j];

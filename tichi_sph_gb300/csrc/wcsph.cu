@@ -64,8 +64,9 @@ __global__ void __launch_bounds__(kBlock) k_wc_acce(KConst k, FluidBuf F, BoundB
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < h2 && r2 > 0.f) {
-            const float r = sqrtf(r2);
-            const float f = -(pri + prj) * mj * (kwg(r * inv_h) * sig_h) / r;
+            float r;
+            const float ri = pair_rinv_pos(r2, r);  // rsqrt pair geometry, as the other sweeps
+            const float f = -(pri + prj) * mj * (kwg(r * inv_h) * sig_h) * ri;
             ax += f * dx;
             ay += f * dy;
             az += f * dz;
