@@ -156,11 +156,13 @@ struct Pair {
         y = pi.y - pj.y;
         z = pi.z - pj.z;
         r2 = x * x + y * y + z * z;
-        const float r = sqrtf(r2);
+        // r and 1 / r from rsqrt, as the forward sweeps (within a few ulp)
+        float r;
+        const float ri = pair_rinv_pos(r2, r);
         const float q = r * v.inv_h;
-        g = kwg(q) * v.sig_h / r;
+        g = kwg(q) * v.sig_h * ri;
         W2 = kwgg(q) * v.sig_h * v.inv_h;
-        G2 = (W2 - g) / r2;
+        G2 = (W2 - g) * (ri * ri);
     }
     __device__ __forceinline__ float dot(float ax, float ay, float az) const { return x * ax + y * ay + z * az; }
 };
