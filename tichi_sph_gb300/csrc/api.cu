@@ -439,6 +439,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     F.zeta = A.get<float>(fcap);
     F.flagpass = A.get<int>(fcap);
     F.nbr = A.get<int>((long long)k.nbr_max * fcap);
+    F.pk = A.get<float4>(fcap);
     F.nbr_cnt = A.get<unsigned int>(fcap);
     F.wcp = ps[0].wcsph_enabled ? A.get<float2>(fcap) : nullptr;
     BoundBuf &B = c.B;
@@ -457,6 +458,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     B.comp = A.get<float>(bcap);
     B.a2 = A.get<float>(bcap);
     B.alpha = A.get<float>(bcap);
+    B.pk = A.get<float4>(bcap);
     B.wcp2 = ps[0].wcsph_enabled ? A.get<float>(bcap) : nullptr;
     c.S.partials_len = 2 * 8 * ((fcap + bcap) / kBlock) + 2 * ublk + 64;  // up to 8 threads per particle
     c.S.partials = A.get<double>(c.S.partials_len);

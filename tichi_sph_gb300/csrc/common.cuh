@@ -178,6 +178,7 @@ struct FluidBuf {
     float4 *vel;       // velocity after the divergence solve
     float4 *vadv;      // two buffers of cap: v_adv ping-pong
     float *psiadv, *kappa;   // psi_adv and psi_adv / alpha
+    float4 *pk;              // (x, y, z, kappa): what the velocity sweep reads of a neighbour
     float4 *acc;       // acce_adv
     float4 *normal;
     float *W, *rho, *comp, *a2;
@@ -204,6 +205,7 @@ struct BoundBuf {
     float2 *mv;        // mass, rest_volume
     float4 *vadv;      // boundary vel_adv (never advanced by the reference)
     float *kappa;      // psi_adv / alpha of the boundary particle
+    float4 *pk;        // (x, y, z, kappa) of the boundary particle
     float *W, *rho, *comp, *a2, *alpha;
     float *wcp2;       // pressure / rho^2 of the boundary particle (weakly compressible block)
 };

@@ -254,8 +254,10 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
             // IPPE_adv_psi_init + IPPE_psi_adv_non_negative, as k_psi
             float pa = (psi - mp.z) + pacc * k.sp[sc].dt;
             if (pa < 0.f) pa = 0.f;
+            const float kap = pa / alpha;
             F.psiadv[s] = pa;
-            F.kappa[s] = pa / alpha;
+            F.kappa[s] = kap;
+            F.pk[s] = make_float4(pi.x, pi.y, pi.z, kap);
             contrib = (double)(pa / mp.z);
         }
     }
@@ -337,7 +339,9 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_bound(KConst k, FluidBuf 
     B.comp[s] = comp;
     B.a2[s] = a2;
     B.alpha[s] = alpha;
-    B.kappa[s] = B.kappa[s] / alpha;  // boundary psi_adv / alpha (psi_adv is never advanced)
+    const float kb = B.kappa[s] / alpha;  // boundary psi_adv / alpha (psi_adv is never advanced)
+    B.kappa[s] = kb;
+    B.pk[s] = make_float4(pi.x, pi.y, pi.z, kb);
 }
 
 // ----------------------------------------------------------------------------- solver
@@ -439,8 +443,10 @@ __global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBu
         const float4 mp = F.mpsi[s];
         float psi = (mp.y - mp.z) + acc * k.sp[sc].dt;
         if (psi < 0.f) psi = 0.f;
+        const float kap = psi / mp.w;
         F.psiadv[s] = psi;
-        F.kappa[s] = psi / mp.w;
+        F.kappa[s] = kap;
+        F.pk[s] = make_float4(pi.x, pi.y, pi.z, kap);
         contrib = (double)(psi / mp.z);
     }
     double bsum;
@@ -483,38 +489,41 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
         Geo g;
         g.load(c, k.R);
         const int cur = st.cur;
-        float ax = 0.f, ay = 0.f, az = 0.f;
+        // IPPE_update_vel_adv's pair term (kappa_i X_j + kappa_j X_i) g x_ij, g =
+        // W'(r) / r, summed as kappa_i alpha_1,i + X_i sum_j kappa_j g x_ij:
+        // alpha_1 = sum_j X_j g x_ij over the same pairs is the density sweep's,
+        // and the second sum needs of a neighbour only (x, y, z, kappa), one
+        // float4 written by the psi sweep (the boundary's by its density sweep)
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
         if (act) {
-            const float4 pi = F.pos[s];
-            const float ki = F.kappa[s];
-            const float Xi = pi.w;
-            // IPPE_update_vel_adv pair term; list entries load both neighbour arrays at once
+            pi = F.pos[s];
             // (valid = false: a padding call of a list block, computed and dropped)
-            auto term = [&](const float4 *P, const float *K, int j, auto listed, bool valid) {
+            auto term = [&](const float4 *PK, int j, auto listed, bool valid) {
                 constexpr bool L = decltype(listed)::value;
-                const float4 pj = P[j];
-                float kj = 0.f;
-                if (L) kj = K[j];
-                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                const float4 qj = PK[j];
+                const float dx = pi.x - qj.x, dy = pi.y - qj.y, dz = pi.z - qj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (L || (r2 < g.h2 && r2 > 0.f)) {
-                    if (!L) kj = K[j];
                     float r;
                     const float ri = L ? pair_rinv_pos(r2, r) : pair_rinv(r2, r);
-                    const float f = (ki * pj.w + kj * Xi) * (kwg(r * g.inv_h) * g.sig_h * ri);
-                    ax = valid ? ax + f * dx : ax;
-                    ay = valid ? ay + f * dy : ay;
-                    az = valid ? az + f * dz : az;
+                    const float f = qj.w * (kwg(r * g.inv_h) * g.sig_h * ri);
+                    sx = valid ? sx + f * dx : sx;
+                    sy = valid ? sy + f * dy : sy;
+                    sz = valid ? sz + f * dz : sz;
                 }
             };
             for_each_neighbor_tpp<DIM, true, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
-                [&](int j, auto listed, bool v) { term(F.pos, F.kappa, j, listed, v); },
-                [&](int j, auto listed, bool v) { term(B.pos, B.kappa, j, listed, v); });
+                [&](int j, auto listed, bool v) { term(F.pk, j, listed, v); },
+                [&](int j, auto listed, bool v) { term(B.pk, j, listed, v); });
         }
-        ax = ln.sum(ax);
-        ay = ln.sum(ay);
-        az = ln.sum(az);
+        sx = ln.sum(sx);
+        sy = ln.sum(sy);
+        sz = ln.sum(sz);
         if (act && ln.q == 0) {
+            const float ki = F.kappa[s], Xi = pi.w;
+            const float4 a1 = F.a1[s];
+            const float ax = ki * a1.x + Xi * sx, ay = ki * a1.y + Xi * sy, az = ki * a1.z + Xi * sz;
             const float4 *vin = F.vadv + cur * F.cap;
             float4 *vout = F.vadv + (1 - cur) * F.cap;
             const float sc_ = -(1.f / k.sp[sc].dt) / F.mpsi[s].x;
