@@ -62,8 +62,8 @@ ALGO_BYTES_3D = {
 # a candidate test (dx, r^2) 8; a fluid particle's pair in the density sweep's
 # list pass 50 with a fluid neighbour, 44 with a boundary one (it recomputes the
 # test); a boundary particle's pair beyond its candidate test 19 with a boundary
-# neighbour, 34 with a fluid one; a list pair in psi 32 and in vel 31.
-FLOPS = {"cand": 8, "dens_ff": 50, "dens_fb": 44, "dens_bb": 19, "dens_bf": 34, "psi": 32, "vel": 31}
+# neighbour, 34 with a fluid one; a list pair in psi 32 and in vel 28.
+FLOPS = {"cand": 8, "dens_ff": 50, "dens_fb": 44, "dens_bb": 19, "dens_bf": 34, "psi": 32, "vel": 28}
 
 
 def alu_roofline(solver, ph, top):
