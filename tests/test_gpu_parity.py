@@ -340,3 +340,52 @@ def test_iteration_floor_and_carried_compression(iter_min, carried):
         assert iters[0][0] >= 1
     if iter_min == 1:
         assert all(d >= 1 and i >= 1 for d, i in iters)
+
+
+def _state_in(fl, bd):
+    nf, nb = fl.part_num[None], bd.part_num[None]
+    fa = {k: getattr(fl, k)[:nf].cpu().numpy().copy() for k in G.STATE_IN}
+    ba = {k: getattr(bd, k)[:nb].cpu().numpy().copy() for k in G.STATE_IN}
+    return fa, ba
+
+
+def _step_outputs(fl, bd):
+    nf, nb = fl.part_num[None], bd.part_num[None]
+    out = {"fluid " + k: getattr(fl, k)[:nf].cpu().numpy().copy()
+           for k in ("pos", "vel", "volume_frac", "W", "sph_density", "sph_compression", "psi_adv", "alpha")}
+    out.update({"bound " + k: getattr(bd, k)[:nb].cpu().numpy().copy() for k in BOUND_FIELDS})
+    return out
+
+
+@pytest.mark.parametrize("scene", ["dfsph3d", "vfsph2d", "wcsph3d"])
+def test_static_boundary_sums_kept_across_substeps(scene):
+    """The boundary particles' sums over boundary neighbours are kept from the
+    previous substep while the gather finds every boundary position and mass
+    bitwise unchanged (the boundary adds them before its fluid terms).  A
+    substep that kept them equals, bit for bit, the same substep in a fresh
+    context, which computes them; so does a substep after the caller moved one
+    boundary particle and changed another's mass."""
+    _need_cuda()
+    init, _ = G.load(scene)
+    cfg, fl, bd, solver = make_gpu(scene, G.init_arrays(init, "fluid"), G.init_arrays(init, "bound"))
+    try:
+        solver.substep()
+        for case in ("unchanged", "moved"):
+            before = solver.stats()
+            if case == "moved":
+                bd.pos[0, 0] += 0.25 * float(cfg.part_size[1])
+                bd.mass[1] *= 1.5
+            fa, ba = _state_in(fl, bd)
+            solver.substep()
+            got, got_st = _step_outputs(fl, bd), solver.stats()
+            _, fl2, bd2, fresh = make_gpu(scene, fa, ba)
+            fresh.set_state(time_count=before["time_count"], compression=before["compression"])
+            fresh.substep()
+            want, want_st = _step_outputs(fl2, bd2), fresh.stats()
+            fresh.close()
+            for k in want:
+                np.testing.assert_array_equal(got[k], want[k], err_msg="%s %s %s" % (scene, case, k))
+            for k in ("div_iter", "incom_iter", "compression", "kinetic_energy", "dt"):
+                assert got_st[k] == want_st[k], (scene, case, k, got_st[k], want_st[k])
+    finally:
+        solver.close()

@@ -459,6 +459,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     B.a2 = A.get<float>(bcap);
     B.alpha = A.get<float>(bcap);
     B.pk = A.get<float4>(bcap);
+    B.bb = A.get<float4>(bcap);
     B.wcp2 = ps[0].wcsph_enabled ? A.get<float>(bcap) : nullptr;
     c.S.partials_len = 2 * 8 * ((fcap + bcap) / kBlock) + 2 * ublk + 64;  // up to 8 threads per particle
     c.S.partials = A.get<double>(c.S.partials_len);

@@ -63,6 +63,10 @@ struct ScenePersist {
     long long total_div_iter, total_incom_iter, total_fbm_passes;
     float dt;
     int32_t steps;
+    // 1 once BoundBuf::bb holds the boundary-boundary sums of the scene's
+    // boundary as gathered (bb_n particles)
+    int32_t bb_valid, pad1;
+    long long bb_n;
 };
 
 // Scalars of a scene for one step; zeroed at the start of every step.
@@ -77,7 +81,9 @@ struct SceneStep {
     int32_t f_in, b_in;         // particles in the grid
     // 1 while psi_adv, kappa and psi_sum of the divergence solve's first
     // iteration come from the density sweep (its psi sweep then does nothing)
-    int32_t psi_ready, pad0;
+    // b_dirty: 1 when this step's gather found a boundary position or mass that
+    // differs bitwise from the previous gather's
+    int32_t psi_ready, b_dirty;
     long long f_shift, b_shift; // sorted slot of global scan position p is p + shift
     unsigned int ticket[6];     // block tickets of this scene (psi, vel, fbm, update)
     double psi_sum, kinetic_energy, potential_energy;
@@ -208,6 +214,10 @@ struct BoundBuf {
     float4 *pk;        // (x, y, z, kappa) of the boundary particle
     float *W, *rho, *comp, *a2, *alpha;
     float *wcp2;       // pressure / rho^2 of the boundary particle (weakly compressible block)
+    // (W, density, compression) summed over the particle's boundary neighbours
+    // alone: the boundary sums add these terms before the fluid's, so a copy
+    // taken while positions and masses stay bitwise the same gives the same bits
+    float4 *bb;
 };
 
 struct Scratch {

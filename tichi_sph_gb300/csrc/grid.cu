@@ -327,14 +327,24 @@ template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, BoundBuf B) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (s >= B.cap) return;
-    const SceneConst &c = k.sc[k.b_chunk_scene[s / kChunk]];
+    const int sc = k.b_chunk_scene[s / kChunk];
+    const SceneConst &c = k.sc[sc];
     if (s - c.b_slot >= c.b_n) return;
     const int pid = B.perm[s];
     B.inv[pid] = (int)s;
     const float *p = U.pos + (int64_t)pid * DIM;
     const float *va = U.vel_adv + (int64_t)pid * DIM;
     const float m = U.mass[pid], V = U.rest_volume[pid];
-    B.pos[s] = make_float4(p[0], p[1], DIM == 3 ? p[2] : 0.f, k.vfsph ? V : m);
+    const float4 np = make_float4(p[0], p[1], DIM == 3 ? p[2] : 0.f, k.vfsph ? V : m);
+    const float4 op = B.pos[s];
+    const float2 omv = B.mv[s];
+    // the slot's previous contents: equal everywhere means the same sorted
+    // order, grid and boundary-boundary sums as the previous gather
+    const bool same = __float_as_uint(op.x) == __float_as_uint(np.x) && __float_as_uint(op.y) == __float_as_uint(np.y) &&
+                      __float_as_uint(op.z) == __float_as_uint(np.z) && __float_as_uint(op.w) == __float_as_uint(np.w) &&
+                      __float_as_uint(omv.x) == __float_as_uint(m) && __float_as_uint(omv.y) == __float_as_uint(V);
+    if (!same) k.ss[sc].b_dirty = 1;
+    B.pos[s] = np;
     B.mv[s] = make_float2(m, V);
     B.vadv[s] = make_float4(va[0], va[1], DIM == 3 ? va[2] : 0.f, 0.f);
     B.kappa[s] = U.psi_adv[pid];  // divided by alpha once alpha is known

@@ -290,6 +290,10 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_bound(KConst k, FluidBuf 
     const SceneConst &c = scene<M>(k, sc);
     if (s - c.b_slot >= c.b_n) return;
     const SceneStep &st = k.ss[sc];
+    const ScenePersist &sp = k.sp[sc];
+    // the (b,b) terms of the last sweep still hold when the gather found every
+    // boundary position and mass unchanged (a static boundary)
+    const bool cached = sp.bb_valid && !st.b_dirty && sp.bb_n == c.b_n;
     Geo g;
     g.load(c, k.R);
     const float4 pi = B.pos[s];
@@ -297,20 +301,28 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_bound(KConst k, FluidBuf 
     const long long code = cell_code<DIM>(pi, g, ok);
     float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f;
     if (ok) {
-        visit_candidates_within<DIM>(B.start, g, pi, code, shift_of<M>(st.b_shift), 0, [&](int j) {
-            const float4 pj = B.pos[j];
-            const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < g.h2) {
-                const float2 mv = B.mv[j];
-                float r;
-                pair_rinv(r2, r);
-                const float w = kw(r * g.inv_h) * g.sig;
-                wsum += w;
-                rho += w * mv.x;
-                comp += w * mv.y;
-            }
-        });
+        if (cached) {
+            const float4 bb = B.bb[s];
+            wsum = bb.x;
+            rho = bb.y;
+            comp = bb.z;
+        } else {
+            visit_candidates_within<DIM>(B.start, g, pi, code, shift_of<M>(st.b_shift), 0, [&](int j) {
+                const float4 pj = B.pos[j];
+                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 < g.h2) {
+                    const float2 mv = B.mv[j];
+                    float r;
+                    pair_rinv(r2, r);
+                    const float w = kw(r * g.inv_h) * g.sig;
+                    wsum += w;
+                    rho += w * mv.x;
+                    comp += w * mv.y;
+                }
+            });
+            B.bb[s] = make_float4(wsum, rho, comp, 0.f);
+        }
         visit_candidates_within<DIM>(F.start, g, pi, code, shift_of<M>(st.f_shift), 0, [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -725,8 +737,17 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
 
 // The boundary particles' own sums run on the side stream beside the fluid
 // sweep: neither writes what the other reads.
+// After k_density_bound: BoundBuf::bb now holds every scene's current
+// boundary-boundary sums.
+__global__ void k_bb_mark(KConst k) {
+    for (int s = threadIdx.x; s < k.n_scenes; s += blockDim.x) {
+        k.sp[s].bb_valid = 1;
+        k.sp[s].bb_n = k.sc[s].b_n;
+    }
+}
+
 void launch_density(tsph_ctx &c, cudaStream_t st) {
-    c.launches += 2;
+    c.launches += 3;
     cudaStream_t sd = c.side ? c.side : st;
     fork_side(c, st);
     TSPH_M_DISPATCH(c.n_scenes > 1,
@@ -737,6 +758,7 @@ void launch_density(tsph_ctx &c, cudaStream_t st) {
             k_density_bound<2, M><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, c.F, c.B);
             k_density_fluid<2, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
         })
+    k_bb_mark<<<1, 256, 0, sd>>>(c.k);
     join_side(c, st);
 }
 
