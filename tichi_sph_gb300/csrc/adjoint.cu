@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kBlock) k_tape_state(KConst k, FluidBuf F, Bou
         a.pos[o] = F.pos[s];
         a.mpsi[o] = F.mpsi[s];
         a.a1[o] = F.a1[s];
-        a.a2[o] = F.a2[s];
+        a.a2[o] = F.dens[s].w;
         a.rho0[o] = F.rho0[s];
         const unsigned int pc = F.nbr_cnt[s];
         a.cnt[o] = pc;
@@ -130,7 +130,7 @@ __global__ void k_tape_end(KConst k, TapeArrays a) {
 __global__ void __launch_bounds__(kBlock) k_density_out(KConst k, FluidBuf F, float *out) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (s >= k.s0.f_n) return;
-    out[F.perm[s]] = F.rho[s];
+    out[F.perm[s]] = F.dens[s].y;
 }
 
 // ----------------------------------------------------------------------------- reverse

@@ -427,10 +427,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     F.kappa = A.get<float>(fcap);
     F.acc = A.get<float4>(fcap);
     F.normal = A.get<float4>(fcap);
-    F.W = A.get<float>(fcap);
-    F.rho = A.get<float>(fcap);
-    F.comp = A.get<float>(fcap);
-    F.a2 = A.get<float>(fcap);
+    F.dens = A.get<float4>(fcap);
     F.a1 = A.get<float4>(fcap);
     F.vf = A.get<float>(P * fcap);
     F.vftmp = A.get<float>(P * fcap);
@@ -453,10 +450,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     B.mv = A.get<float2>(bcap);
     B.vadv = A.get<float4>(bcap);
     B.kappa = A.get<float>(bcap);
-    B.W = A.get<float>(bcap);
-    B.rho = A.get<float>(bcap);
-    B.comp = A.get<float>(bcap);
-    B.a2 = A.get<float>(bcap);
+    B.dens = A.get<float4>(bcap);
     B.alpha = A.get<float>(bcap);
     B.pk = A.get<float4>(bcap);
     B.bb = A.get<float4>(bcap);

@@ -187,7 +187,7 @@ struct FluidBuf {
     float4 *pk;              // (x, y, z, kappa): what the velocity sweep reads of a neighbour
     float4 *acc;       // acce_adv
     float4 *normal;
-    float *W, *rho, *comp, *a2;
+    float4 *dens;      // W, sph_density, sph_compression, alpha_2: read together by the write-back
     float4 *a1;
     float *vf, *vftmp;       // [P][cap]
     float4 *drift;           // [P][cap]
@@ -212,7 +212,8 @@ struct BoundBuf {
     float4 *vadv;      // boundary vel_adv (never advanced by the reference)
     float *kappa;      // psi_adv / alpha of the boundary particle
     float4 *pk;        // (x, y, z, kappa) of the boundary particle
-    float *W, *rho, *comp, *a2, *alpha;
+    float4 *dens;      // W, sph_density, sph_compression, alpha_2
+    float *alpha;
     float *wcp2;       // pressure / rho^2 of the boundary particle (weakly compressible block)
     // (W, density, compression) summed over the particle's boundary neighbours
     // alone: the boundary sums add these terms before the fluid's, so a copy

@@ -373,6 +373,7 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
         const float dt = k.sp[sc].dt;
         const float4 v = F.vadv[st.cur * F.cap + s];
         const float4 p = F.pos[s];
+        const float4 dn = F.dens[s];
         const float V = F.mv[s].y;
         const int flagged = fbm ? (F.flagpass[s] != 0) : 0;
         float rho0 = 0.f;
@@ -424,13 +425,13 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
         U.flag[pid] = flagged;
         U.mass[pid] = m;
         U.rest_density[pid] = rho0;
-        U.W[pid] = F.W[s];
-        U.sph_density[pid] = F.rho[s];
-        U.sph_compression[pid] = F.comp[s];
+        U.W[pid] = dn.x;
+        U.sph_density[pid] = dn.y;
+        U.sph_compression[pid] = dn.z;
         U.psi_adv[pid] = F.psiadv[s];
         if (F.wcp && U.pressure) U.pressure[pid] = F.wcp[s].x;
         U.alpha[pid] = F.mpsi[s].w;
-        U.alpha_2[pid] = F.a2[s];
+        U.alpha_2[pid] = dn.w;
         if (s - c.f_slot < st.f_in) {
             // slot in the reference's combined grid: cell offset over both sets, fluid first
             const int code = U.neighb_cell_seq[pid];
@@ -481,10 +482,11 @@ __global__ void __launch_bounds__(kBlock) k_update_bound(KConst k, tsph_set U, B
     const SceneConst &c = k.sc[sc];
     const SceneStep &st = k.ss[sc];
     const int64_t s = B.inv[pid];
-    U.W[pid] = B.W[s];
-    U.sph_density[pid] = B.rho[s];
-    U.sph_compression[pid] = B.comp[s];
-    U.alpha_2[pid] = B.a2[s];
+    const float4 d = B.dens[s];
+    U.W[pid] = d.x;
+    U.sph_density[pid] = d.y;
+    U.sph_compression[pid] = d.z;
+    U.alpha_2[pid] = d.w;
     U.alpha[pid] = B.alpha[s];
     if (s - c.b_slot < st.b_in) {
         const int code = U.neighb_cell_seq[pid];

@@ -240,11 +240,8 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
         const float4 mp = F.mpsi[s];
         float alpha = (a1x * a1x + a1y * a1y + a1z * a1z) / mp.x + a2;
         if (alpha < 1e-4f) alpha = 1e-4f;
-        F.W[s] = wsum;
-        F.rho[s] = rho;
-        F.comp[s] = comp;
+        F.dens[s] = make_float4(wsum, rho, comp, a2);
         F.a1[s] = make_float4(a1x, a1y, a1z, 0.f);
-        F.a2[s] = a2;
         const float psi = k.vfsph ? comp : rho;
         F.mpsi[s] = make_float4(mp.x, psi, mp.z, alpha);
         // psi also rides in the current v_adv's unused w (the velocity sweeps carry
@@ -346,10 +343,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_bound(KConst k, FluidBuf 
     const float m = B.mv[s].x;
     float alpha = 0.f / m + a2;
     if (alpha < 1e-4f) alpha = 1e-4f;
-    B.W[s] = wsum;
-    B.rho[s] = rho;
-    B.comp[s] = comp;
-    B.a2[s] = a2;
+    B.dens[s] = make_float4(wsum, rho, comp, a2);
     B.alpha[s] = alpha;
     const float kb = B.kappa[s] / alpha;  // boundary psi_adv / alpha (psi_adv is never advanced)
     B.kappa[s] = kb;

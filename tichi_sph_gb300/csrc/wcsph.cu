@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(kBlock) k_wc_pressure(KConst k, FluidBuf F, Bo
     if (s < F.cap) {
         const SceneConst &c = scene<M>(k, f_block_scene<M>(k, s - (s % kChunk)));
         if (s - c.f_slot < c.f_n) {
-            const float rho = F.rho[s], rho0 = F.rho0[s];
+            const float rho = F.dens[s].y, rho0 = F.rho0[s];
             float p = (rho0 * (float)(c.cs * c.cs)) / (float)c.wc_gamma * (pow7(rho / rho0) - 1.f);
             if (p < 0.f) p = 0.f;
             F.wcp[s] = make_float2(p, p / (rho * rho));
@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kBlock) k_wc_pressure(KConst k, FluidBuf F, Bo
         const SceneConst &c = scene<M>(k, b_block_scene<M>(k, s - (s % kChunk)));
         if (s - c.b_slot < c.b_n) {
             const float p = bpress ? bpress[B.perm[s]] : 0.f;
-            const float rho = B.rho[s];
+            const float rho = B.dens[s].y;
             B.wcp2[s] = p / (rho * rho);
         }
     }
