@@ -481,6 +481,12 @@ __global__ void __launch_bounds__(kBlock) k_update_bound(KConst k, tsph_set U, B
     const int sc = k.b_user_scene[pid];
     const SceneConst &c = k.sc[sc];
     const SceneStep &st = k.ss[sc];
+    if (pid == c.b_user) {
+        // the density sweep of this step has run: BoundBuf::bb holds the
+        // boundary-boundary sums of the boundary as gathered
+        k.sp[sc].bb_valid = 1;
+        k.sp[sc].bb_n = c.b_n;
+    }
     const int64_t s = B.inv[pid];
     const float4 d = B.dens[s];
     U.W[pid] = d.x;

@@ -731,17 +731,8 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
 
 // The boundary particles' own sums run on the side stream beside the fluid
 // sweep: neither writes what the other reads.
-// After k_density_bound: BoundBuf::bb now holds every scene's current
-// boundary-boundary sums.
-__global__ void k_bb_mark(KConst k) {
-    for (int s = threadIdx.x; s < k.n_scenes; s += blockDim.x) {
-        k.sp[s].bb_valid = 1;
-        k.sp[s].bb_n = k.sc[s].b_n;
-    }
-}
-
 void launch_density(tsph_ctx &c, cudaStream_t st) {
-    c.launches += 3;
+    c.launches += 2;
     cudaStream_t sd = c.side ? c.side : st;
     fork_side(c, st);
     TSPH_M_DISPATCH(c.n_scenes > 1,
@@ -752,7 +743,6 @@ void launch_density(tsph_ctx &c, cudaStream_t st) {
             k_density_bound<2, M><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, c.F, c.B);
             k_density_fluid<2, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
         })
-    k_bb_mark<<<1, 256, 0, sd>>>(c.k);
     join_side(c, st);
 }
 
