@@ -181,22 +181,22 @@ def _ncu_traffic(kernel):
     return None
 
 
-def build_sim(n_side, device):
+def build_sim(n_side, device, spacing=0.01):
     from tichi_sph_gb300 import sph_config, workloads
     from tichi_sph_gb300.simulation import Simulation
-    cfg_d, scen_d = workloads.dambreak_3d(n_side)
+    cfg_d, scen_d = workloads.dambreak_3d(n_side, spacing)
     cfg = sph_config.Config(cfg_d, scen_d)
     sim = Simulation(cfg, device=device)
     sim.init_scenario()
     return cfg, sim
 
 
-def cpu_baseline(n_side, budget_s, max_steps):
+def cpu_baseline(n_side, budget_s, max_steps, spacing=0.01):
     """C restatement of the reference (FP32, OpenMP) on the same initial state."""
     from oracle.port import PortSim
     from tichi_sph_gb300 import sph_config, workloads
     from tichi_sph_gb300.simulation import Simulation
-    cfg_d, scen_d = workloads.dambreak_3d(n_side)
+    cfg_d, scen_d = workloads.dambreak_3d(n_side, spacing)
     cfg = sph_config.Config(cfg_d, scen_d)
     sim = Simulation(cfg, device="cpu")
     sim.init_scenario()
@@ -221,7 +221,7 @@ def cpu_baseline(n_side, budget_s, max_steps):
             "sample": "%d substeps of the full scene from rest (%d fluid + %d boundary particles), %.1f s, "
                       "C restatement of the reference kernels (oracle/sph_port.c), FP32" % (
                           steps, nf, sim.bound.part_num[None], el),
-            "ms_per_step": el / steps * 1e3, "iters": iters}
+            "ms_per_step": el / steps * 1e3, "iters": iters, "n_bound": sim.bound.part_num[None]}
 
 
 def run_batched(n_scenes, steps, warmup, dev, dist=None, rank=0, ws=1):
@@ -439,14 +439,15 @@ def run_reference(args, rank, ws):
     if rank != 0:
         return 0
     n_side = args.n_side
-    res = cpu_baseline(n_side, budget_s=args.ref_budget, max_steps=args.warmup + args.steps)
+    res = cpu_baseline(n_side, budget_s=args.ref_budget, max_steps=args.warmup + args.steps, spacing=args.spacing)
     nf = n_side ** 3
     line = {
         "metric": METRIC, "value": res["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": len(res["iters"]), "warmup": 0, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "3D DFSPH dam break, %d fluid + 566742 boundary particles, h=0.02, "
-                               "dt<=2e-4, rho tol 0.1%%" % nf, "fluid_particles": nf},
+        "config": {"workload": "3D DFSPH dam break, %d fluid + %d boundary particles, h=%g, "
+                               "dt<=%g, rho tol 0.1%%" % (nf, res["n_bound"], 2 * args.spacing, args.spacing / 50),
+                   "fluid_particles": nf},
         "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "Taichi (the reference's kernel compiler) is not installed; the reference's kernel sequence "
@@ -463,6 +464,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-side", type=int, default=100)
+    ap.add_argument("--spacing", type=float, default=0.01,
+                    help="particle spacing of the 3D dam break (the cube is n-side particles wide, the tank fixed)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
@@ -512,7 +515,7 @@ def main():
         if dist:
             dist.destroy_process_group()
         return 0
-    cfg, sim = build_sim(args.n_side, dev)
+    cfg, sim = build_sim(args.n_side, dev, args.spacing)
     solver = sim.solver
     if args.hostloop:
         solver.set_graph_mode(False)
@@ -640,7 +643,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cb = cpu_baseline(args.n_side, budget_s=args.cpu_budget, max_steps=20)
+        cb = cpu_baseline(args.n_side, budget_s=args.cpu_budget, max_steps=20, spacing=args.spacing)
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     if rank == 0:
@@ -648,12 +651,13 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "3D DFSPH dam break, %d fluid + %d boundary particles, h=0.02, dt<=2e-4 (CFL), "
-                                   "rho tol 0.1%%, div tol 1%%, from rest" % (nf, nb),
+            "config": {"workload": "3D DFSPH dam break, %d fluid + %d boundary particles, h=%g, dt<=%g (CFL), "
+                                   "rho tol 0.1%%, div tol 1%%, from rest" % (nf, nb, 2 * args.spacing,
+                                                                             args.spacing / 50),
                        "fluid_particles": nf, "boundary_particles": nb, "parallelism": "replicas" if ws > 1 else "single",
                        "mean_div_iter": k_div, "mean_incom_iter": k_inc,
                        "max_density_error": s1["max_dens_compression"],
-                       "l2": "inputs larger than L2 (per-step state ~400 MB > 129 MB)",
+                       "l2": "inputs larger than L2 (per-step state ~%d MB > 129 MB)" % round(400 * nf / 1e6),
                        "threads_per_particle": solver.tpp, "autotune_ms": tune,
                        "graph": "host-driven solver loops" if args.hostloop else
                        "one CUDA graph per substep, device-side while nodes"},

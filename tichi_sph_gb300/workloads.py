@@ -62,10 +62,16 @@ def dambreak_3d(n_side=100, spacing=0.01):
                     "gravity": [0, -9.81, 0], "phase_num": 1, "phase_rest_density": [1000],
                     "phase_color_hex": ["0x6F7DBC"]},
         "fluid": {"max_part_num": n_side ** 3, "objs": [_obj("cube", [0.0, 0.0, 0.0], [L, L, L], [1], [0, 0, 0])]},
-        "bound": {"max_part_num": 566742, "objs": [
+        "bound": {"max_part_num": _tank_bound_cap(spacing), "objs": [
             _obj("box", [-0.035, -0.035, -0.035], [3.035, 1.535, 1.035], [1], [0, 0, 0], layers=3)]},
     }
     return cfg, scen
+
+
+def _tank_bound_cap(spacing):
+    """Boundary capacity of the 3 x 1.5 x 1 m tank: 566,742 particles at 0.01 m,
+    scaled with the wall area per particle (plus 5%) at other spacings."""
+    return 566742 if spacing == 0.01 else int(566742 * (0.01 / spacing) ** 2 * 1.05)
 
 
 def twophase_3d(n_side=100, spacing=0.01, seed=3):
