@@ -106,3 +106,57 @@ def test_batch_equals_scenes_alone(scene, ks):
             c1, c2 = stats[i]["compression"], st["compression"]
             assert (c1 == c2) or (np.isnan(c1) and np.isnan(c2)), (i, step, c1, c2)
     batch.close()
+
+
+def test_batch_moved_boundary_in_one_scene():
+    """The boundary sums kept across substeps are per scene: after the caller
+    moves a boundary particle of one scene (and changes another's mass), that
+    scene's sums are recomputed and the others' kept, and every scene still
+    equals its solo run bit for bit."""
+    _need_cuda()
+    from tichi_sph_gb300.batch import BatchSolver, gather_scenes
+    variants = [_variant("dfsph3d", k) for k in (0, 1, 2)]
+    moved = 1
+
+    def touch(cfg, bd):
+        bd.pos[0, 0] += 0.25 * float(cfg.part_size[1])
+        bd.mass[1] *= 1.5
+
+    solo = []
+    for i, (cfg, fa, ba) in enumerate(variants):
+        fl, bd, s = _solo(cfg, fa, ba, False)
+        rec = []
+        for step in range(4):
+            if step == 2 and i == moved:
+                touch(cfg, bd)
+            s.substep()
+            st = s.stats()
+            rec.append((fl.pos[:len(fa["pos"])].cpu().numpy().copy(), fl.vel[:len(fa["pos"])].cpu().numpy().copy(),
+                        bd.sph_density[:len(ba["pos"])].cpu().numpy().copy(),
+                        bd.sph_compression[:len(ba["pos"])].cpu().numpy().copy(), st))
+        s.close()
+        solo.append(rec)
+    sims = []
+    for cfg, fa, ba in variants:
+        fl, bd, s = _solo(cfg, fa, ba, False)
+        s.close()
+        sims.append(types.SimpleNamespace(config=cfg, fluid=fl, bound=bd))
+    fluid, bound, nf, nb = gather_scenes(sims)
+    batch = BatchSolver([v[0] for v in variants], fluid, bound, nf, nb)
+    for step in range(4):
+        if step == 2:
+            touch(variants[moved][0], sims[moved].bound)
+        batch.substep()
+        stats = batch.stats()
+        for i, sim in enumerate(sims):
+            pos, vel, brho, bcomp, st = solo[i][step]
+            n, m = nf[i], nb[i]
+            tag = "scene %d step %d" % (i, step)
+            np.testing.assert_array_equal(sim.fluid.pos[:n].cpu().numpy(), pos, err_msg=tag + " pos")
+            np.testing.assert_array_equal(sim.fluid.vel[:n].cpu().numpy(), vel, err_msg=tag + " vel")
+            np.testing.assert_array_equal(sim.bound.sph_density[:m].cpu().numpy(), brho, err_msg=tag + " bound rho")
+            np.testing.assert_array_equal(sim.bound.sph_compression[:m].cpu().numpy(), bcomp,
+                                          err_msg=tag + " bound compression")
+            for key in ("dt", "div_iter", "incom_iter", "compression", "kinetic_energy"):
+                assert stats[i][key] == st[key], (tag, key, stats[i][key], st[key])
+    batch.close()
