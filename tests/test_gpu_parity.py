@@ -364,17 +364,20 @@ def test_static_boundary_sums_kept_across_substeps(scene):
     bitwise unchanged (the boundary adds them before its fluid terms).  A
     substep that kept them equals, bit for bit, the same substep in a fresh
     context, which computes them; so does a substep after the caller moved one
-    boundary particle and changed another's mass."""
+    boundary particle and changed another's mass, and one after such a change
+    was first seen by a call that builds the grid alone (the neighbour stats)."""
     _need_cuda()
     init, _ = G.load(scene)
     cfg, fl, bd, solver = make_gpu(scene, G.init_arrays(init, "fluid"), G.init_arrays(init, "bound"))
     try:
         solver.substep()
-        for case in ("unchanged", "moved"):
+        for case in ("unchanged", "moved", "moved, then the grid alone"):
             before = solver.stats()
-            if case == "moved":
+            if case != "unchanged":
                 bd.pos[0, 0] += 0.25 * float(cfg.part_size[1])
                 bd.mass[1] *= 1.5
+            if case == "moved, then the grid alone":
+                solver.neighbor_stats()
             fa, ba = _state_in(fl, bd)
             solver.substep()
             got, got_st = _step_outputs(fl, bd), solver.stats()

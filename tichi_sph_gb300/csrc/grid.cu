@@ -339,11 +339,16 @@ __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, B
     const float4 op = B.pos[s];
     const float2 omv = B.mv[s];
     // the slot's previous contents: equal everywhere means the same sorted
-    // order, grid and boundary-boundary sums as the previous gather
+    // order, grid and boundary-boundary sums as the previous gather.  A change
+    // also drops the kept sums for good, so that a later step cannot take them
+    // after a call that gathered without a density sweep (the neighbour stats)
     const bool same = __float_as_uint(op.x) == __float_as_uint(np.x) && __float_as_uint(op.y) == __float_as_uint(np.y) &&
                       __float_as_uint(op.z) == __float_as_uint(np.z) && __float_as_uint(op.w) == __float_as_uint(np.w) &&
                       __float_as_uint(omv.x) == __float_as_uint(m) && __float_as_uint(omv.y) == __float_as_uint(V);
-    if (!same) k.ss[sc].b_dirty = 1;
+    if (!same) {
+        k.ss[sc].b_dirty = 1;
+        k.sp[sc].bb_valid = 0;
+    }
     B.pos[s] = np;
     B.mv[s] = make_float2(m, V);
     B.vadv[s] = make_float4(va[0], va[1], DIM == 3 ? va[2] : 0.f, 0.f);
