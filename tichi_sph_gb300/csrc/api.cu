@@ -396,7 +396,6 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     std::vector<int> fchunk(fcap / kChunk, 0), bchunk(bcap / kChunk, 0);
     std::vector<int> fus(fuser > 0 ? fuser : 1, 0), bus(buser > 0 ? buser : 1, 0);
     std::vector<int> fub(ublk, 0);
-    std::vector<long long> cb(S + 1);
     for (int s = 0; s < S; ++s) {
         for (long long i = 0; i < sc[s].f_ublks; ++i) fub[sc[s].f_ublk0 + i] = s;
         for (long long i = sc[s].f_slot / kChunk; i < (sc[s].f_slot + sc[s].f_slots) / kChunk; ++i) fchunk[i] = s;
@@ -404,11 +403,9 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
         const long long fu = batch ? sc[s].f_n : capf, bu = batch ? sc[s].b_n : capb;
         for (long long i = 0; i < fu; ++i) fus[sc[s].f_user + i] = s;
         for (long long i = 0; i < bu; ++i) bus[sc[s].b_user + i] = s;
-        cb[s] = sc[s].cbase;
     }
     if (fslot == 0)  // all scenes are without fluid: the chunk belongs to one of them
         for (auto &v : fchunk) v = 0;
-    cb[S] = nn;
 
     FluidBuf &F = c.F;
     F.cap = fcap;
@@ -417,6 +414,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     F.slot = A.get<int>((long long)fus.size());
     F.inv = A.get<int>((long long)fus.size());
     F.perm = A.get<int>(fcap);
+    F.perm_u = A.get<int>(fcap);
     F.pos = A.get<float4>(fcap);
     F.mv = A.get<float2>(fcap);
     F.mpsi = A.get<float4>(fcap);
@@ -446,6 +444,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     B.slot = A.get<int>((long long)bus.size());
     B.inv = A.get<int>((long long)bus.size());
     B.perm = A.get<int>(bcap);
+    B.perm_u = A.get<int>(bcap);
     B.pos = A.get<float4>(bcap);
     B.mv = A.get<float2>(bcap);
     B.vadv = A.get<float4>(bcap);
@@ -468,14 +467,12 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     int *d_bchunk = A.get<int>((long long)bchunk.size());
     int *d_fus = A.get<int>((long long)fus.size());
     int *d_bus = A.get<int>((long long)bus.size());
-    long long *d_cb = A.get<long long>(S + 1);
     int *d_fub = A.get<int>(ublk);
     k.sc = d_sc;
     k.f_chunk_scene = d_fchunk;
     k.b_chunk_scene = d_bchunk;
     k.f_user_scene = d_fus;
     k.b_user_scene = d_bus;
-    k.cbase_list = d_cb;
     k.f_ublock_scene = d_fub;
     k.f_ublocks = ublk;
     k.s0 = sc[0];
@@ -485,7 +482,6 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     if (e == cudaSuccess) e = cudaMemcpy(d_bchunk, bchunk.data(), sizeof(int) * bchunk.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_fus, fus.data(), sizeof(int) * fus.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_bus, bus.data(), sizeof(int) * bus.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_cb, cb.data(), sizeof(long long) * (S + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_fub, fub.data(), sizeof(int) * ublk, cudaMemcpyHostToDevice);
     void *hp = nullptr;
     if (e == cudaSuccess) e = cudaMallocHost(&hp, sizeof(SceneConst) * S);

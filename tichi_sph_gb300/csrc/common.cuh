@@ -112,7 +112,6 @@ struct KConst {
     const int *b_chunk_scene;
     const int *f_user_scene;              // scene of each caller-order particle
     const int *b_user_scene;
-    const long long *cbase_list;          // cbase of every scene, then total_nodes
     const int *f_ublock_scene;            // scene of each caller-order block of kBlock
     long long f_ublocks;
     SceneConst s0;                        // scene 0 by value (the one-scene kernels read it here)
@@ -177,6 +176,7 @@ __host__ __device__ __forceinline__ int64_t nbr_index(int t, int64_t s, int64_t 
 struct FluidBuf {
     int64_t cap;             // padded slots over all scenes
     int *count, *start, *slot, *perm, *inv;
+    int *perm_u;             // particle ids in scatter order (each cell's ids unordered)
     float4 *pos;       // x, y, z, X (mass for DFSPH, rest_volume for VFSPH)
     float2 *mv;        // mass, rest_volume
     float4 *mpsi;      // mass, psi (sph_psi), psi0 (rest_psi), alpha
@@ -207,6 +207,7 @@ struct FluidBuf {
 struct BoundBuf {
     int64_t cap;
     int *count, *start, *slot, *perm, *inv;
+    int *perm_u;       // particle ids in scatter order (each cell's ids unordered)
     float4 *pos;       // x, y, z, X
     float2 *mv;        // mass, rest_volume
     float4 *vadv;      // boundary vel_adv (never advanced by the reference)
@@ -671,17 +672,6 @@ __device__ __forceinline__ void for_each_neighbor_tpp(const SceneConst &c, const
             if (BOUND) visit_candidates_lean<DIM, TPP>(B.start, &c, R, code, st.b_shift, q, fbs);
         }
     }
-}
-
-// Scene of a global cell code (binary search over the scenes' cbase list).
-__device__ __forceinline__ int scene_of_cell(const KConst &k, long long code) {
-    int lo = 0, hi = k.n_scenes - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (k.cbase_list[mid] <= code) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
 }
 
 inline int blocks_for(int64_t n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }

@@ -238,66 +238,29 @@ __global__ void __launch_bounds__(kBlock) k_scatter(KConst k, int bound, int64_t
     perm[s] = (int)i;
 }
 
-// Orders each cell's particles by id (insertion sort; cells hold ~2^dim..30),
-// blockIdx.y selecting the grid.
-__device__ __forceinline__ void insertion_sort(int *p, long long beg, long long end) {
-    for (long long a = beg + 1; a < end; ++a) {
-        int v = p[a];
-        long long b = a - 1;
-        while (b >= beg && p[b] > v) {
-            p[b + 1] = p[b];
-            --b;
-        }
-        p[b + 1] = v;
-    }
+// Sorted slot of the particle `pid` found at unsorted slot range [beg, end) of
+// its cell (or of its scene's tail of particles without a valid cell): a cell's
+// particles are ordered by id, so its slot is the range's first slot plus the
+// number of the range's particles with a smaller id.
+__device__ __forceinline__ int64_t sorted_slot(const int *__restrict__ perm_u, int64_t beg, int64_t end, int pid) {
+    int r = 0;
+    for (int64_t a = beg; a < end; ++a) r += perm_u[a] < pid;
+    return beg + r;
 }
 
-// Cells of up to kRegSort particles are sorted in registers: all ids load at
-// once (independent loads, one memory latency), a fixed odd-even transposition
-// network orders them, one write-back; larger cells use insertion_sort.
-constexpr int kRegSort = 16;
-
-// Threads past the last cell sort the scenes' tails of particles without a
-// valid cell, by id (one thread per scene and grid).
-__global__ void __launch_bounds__(kBlock) k_cell_sort(KConst k, const int *__restrict__ fstart, int *fperm,
-                                                      const int *__restrict__ bstart, int *bperm) {
-    const int g = blockIdx.y;
-    const long long c = blockIdx.x * (long long)kBlock + threadIdx.x;
-    if (c >= k.total_nodes) {
-        const long long s = c - k.total_nodes;
-        if (s >= k.n_scenes) return;
-        const SceneConst &sc = k.sc[s];
-        const SceneStep &st = k.ss[s];
-        if (g == 0 && st.f_tail > 1) insertion_sort(fperm, sc.f_slot + st.f_in, sc.f_slot + st.f_in + st.f_tail);
-        if (g == 1 && st.b_tail > 1) insertion_sort(bperm, sc.b_slot + st.b_in, sc.b_slot + st.b_in + st.b_tail);
-        return;
+// The slot range of the cell (in-grid particles, slots [slot0, slot0 + n_in))
+// or of the scene's tail that holds the particle at unsorted slot u; `shift`
+// maps the grid's scan positions to the scene's slots, as in k_scatter.
+__device__ __forceinline__ void slot_range(const SceneConst &c, long long shift, const int *__restrict__ start,
+                                           int64_t u, int64_t slot0, int32_t n_in, int32_t n_tail, int code,
+                                           int64_t &beg, int64_t &end) {
+    if (u - slot0 < n_in) {
+        beg = start[c.cbase + code] + shift;
+        end = start[c.cbase + code + 1] + shift;
+    } else {
+        beg = slot0 + n_in;
+        end = beg + n_tail;
     }
-    const int *start = g ? bstart : fstart;
-    const int beg = start[c], end = start[c + 1];
-    const int n = end - beg;
-    if (n < 2) return;
-    const int sc = scene_of_cell(k, c);
-    const long long shift = g ? k.ss[sc].b_shift : k.ss[sc].f_shift;
-    int *p = (g ? bperm : fperm) + beg + shift;
-    if (n > kRegSort) {
-        insertion_sort(p, 0, n);
-        return;
-    }
-    int v[kRegSort];
-#pragma unroll
-    for (int i = 0; i < kRegSort; ++i) v[i] = i < n ? p[i] : 0x7fffffff;
-#pragma unroll
-    for (int r = 0; r < kRegSort; ++r) {
-#pragma unroll
-        for (int i = r & 1; i + 1 < kRegSort; i += 2) {
-            const int a = min(v[i], v[i + 1]), b = max(v[i], v[i + 1]);
-            v[i] = a;
-            v[i + 1] = b;
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < kRegSort; ++i)
-        if (i < n) p[i] = v[i];
 }
 
 // ----------------------------------------------------------------------------- gather
@@ -306,11 +269,17 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(KConst k, const int *__res
 // sph_obj.py:65-73.
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_gather_fluid(KConst k, tsph_set U, FluidBuf F) {
-    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= F.cap) return;
-    const SceneConst &c = k.sc[k.f_chunk_scene[s / kChunk]];
-    if (s - c.f_slot >= c.f_n) return;
-    const int pid = F.perm[s];
+    const int64_t u = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (u >= F.cap) return;
+    const int sc = k.f_chunk_scene[u / kChunk];
+    const SceneConst &c = k.sc[sc];
+    if (u - c.f_slot >= c.f_n) return;
+    const SceneStep &st = k.ss[sc];
+    const int pid = F.perm_u[u];
+    int64_t beg, end;
+    slot_range(c, st.f_shift, F.start, u, c.f_slot, st.f_in, st.f_tail, U.neighb_cell_seq[pid], beg, end);
+    const int64_t s = sorted_slot(F.perm_u, beg, end, pid);
+    F.perm[s] = pid;
     F.inv[pid] = (int)s;
     const float *p = U.pos + (int64_t)pid * DIM;
     const float *v = U.vel + (int64_t)pid * DIM;
@@ -325,12 +294,17 @@ __global__ void __launch_bounds__(kBlock) k_gather_fluid(KConst k, tsph_set U, F
 
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, BoundBuf B) {
-    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (s >= B.cap) return;
-    const int sc = k.b_chunk_scene[s / kChunk];
+    const int64_t u = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (u >= B.cap) return;
+    const int sc = k.b_chunk_scene[u / kChunk];
     const SceneConst &c = k.sc[sc];
-    if (s - c.b_slot >= c.b_n) return;
-    const int pid = B.perm[s];
+    if (u - c.b_slot >= c.b_n) return;
+    const SceneStep &st = k.ss[sc];
+    const int pid = B.perm_u[u];
+    int64_t beg, end;
+    slot_range(c, st.b_shift, B.start, u, c.b_slot, st.b_in, st.b_tail, U.neighb_cell_seq[pid], beg, end);
+    const int64_t s = sorted_slot(B.perm_u, beg, end, pid);
+    B.perm[s] = pid;
     B.inv[pid] = (int)s;
     const float *p = U.pos + (int64_t)pid * DIM;
     const float *va = U.vel_adv + (int64_t)pid * DIM;
@@ -594,11 +568,10 @@ void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st) {
 
 void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st, bool with_cfl) {
     const int64_t nn = c.k.total_nodes;
-    const int S = c.k.n_scenes;
     // the boundary set's encode, scatter and gather run on the side stream,
-    // beside the fluid's; the scans and sorts cover both grids in one launch
+    // beside the fluid's; the scans cover both grids in one launch
     cudaStream_t sd = c.side ? c.side : st;
-    c.launches += (f.n > 0) + (b.n > 0) + 2 + (f.n > 0) + (b.n > 0) + 1 + 2;
+    c.launches += (f.n > 0) + (b.n > 0) + 2 + (f.n > 0) + (b.n > 0) + 2;
     fork_side(c, st);
     if (with_cfl) launch_cfl(c, f, sd);  // nothing before the first solve reads dt
     cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, sd);
@@ -621,11 +594,10 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     k_scan_reduce<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk, c.k.dg->ticket + kGtScanF);
     k_scan_down<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk, c.k, c.k.dg->ticket + kGtScanDone);
     fork_side(c, st);
-    if (b.n > 0) k_scatter<<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm);
-    if (f.n > 0) k_scatter<<<blocks_for(f.n), kBlock, 0, st>>>(c.k, 0, f.n, f.neighb_cell_seq, c.F.slot, c.F.start, c.F.perm);
-    join_side(c, st);
-    k_cell_sort<<<dim3(blocks_for(nn + S), 2), kBlock, 0, st>>>(c.k, c.F.start, c.F.perm, c.B.start, c.B.perm);
-    fork_side(c, st);
+    if (b.n > 0) k_scatter<<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm_u);
+    if (f.n > 0) k_scatter<<<blocks_for(f.n), kBlock, 0, st>>>(c.k, 0, f.n, f.neighb_cell_seq, c.F.slot, c.F.start, c.F.perm_u);
+    // each set's gather orders its cells by particle id as it copies (a
+    // particle's slot is its rank among its cell's ids)
     if (c.k.dim == 3) {
         k_gather_bound<3><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, b, c.B);
         k_gather_fluid<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F);
