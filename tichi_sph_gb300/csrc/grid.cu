@@ -319,7 +319,11 @@ __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, B
     const bool same = __float_as_uint(op.x) == __float_as_uint(np.x) && __float_as_uint(op.y) == __float_as_uint(np.y) &&
                       __float_as_uint(op.z) == __float_as_uint(np.z) && __float_as_uint(op.w) == __float_as_uint(np.w) &&
                       __float_as_uint(omv.x) == __float_as_uint(m) && __float_as_uint(omv.y) == __float_as_uint(V);
-    if (!same) {
+    // one store per warp that saw a change (a warp lies in one scene's chunk),
+    // none once the flag is up: every slot differs in a first gather or under
+    // a moving boundary, and the stores would all go to one word
+    const unsigned int changed = __ballot_sync(__activemask(), !same);
+    if (changed && (threadIdx.x & 31) == __ffs(changed) - 1 && !__ldcg(&k.ss[sc].b_dirty)) {
         k.ss[sc].b_dirty = 1;
         k.sp[sc].bb_valid = 0;
     }
