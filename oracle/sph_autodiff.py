@@ -55,11 +55,23 @@ def ddw_q(q):
     return torch.where(q <= 0.5, a, torch.where(q < 1, b, torch.zeros_like(q)))
 
 
+def c_q(q):
+    """Cohesion spline shape (``sph_util.py:4-13`` without 32 / (pi h^3))."""
+    p = (1 - q) ** 3 * q ** 3
+    return torch.where(q <= 0.5, 2 * p - 1 / 64, torch.where(q < 1, p, torch.zeros_like(q)))
+
+
+def dc_q(q):
+    """d c_q / dq: 3 q^2 (1 - q)^2 (1 - 2 q), doubled below q = 1/2."""
+    p = 3 * q ** 2 * (1 - q) ** 2 * (1 - 2 * q)
+    return torch.where(q <= 0.5, 2 * p, torch.where(q < 1, p, torch.zeros_like(q)))
+
+
 class Scene:
     """Constants of a differentiable DFSPH scene (one phase, static boundary)."""
 
     def __init__(self, dim, h, sig, mass, rest_density, bpos, bmass, gravity, dt, iters=(2, 2), tol=(1e-2, 1e-3),
-                 iter_max=100, bvel=None):
+                 iter_max=100, bvel=None, gamma=0.0, lb=None):
         self.dim = dim
         self.h = float(h)
         self.sig = float(sig)
@@ -75,6 +87,11 @@ class Scene:
         self.iter_max = int(iter_max)
         self.lap = 2.0 * (2 + dim)
         self.eps = 0.01 * self.h ** 2
+        self.gamma = float(gamma)
+        self.csig = 32.0 / math.pi / self.h ** 3
+        # grid origin: the surface tension's curvature term runs over the
+        # template cells' candidates (cell = h), not only pairs within h
+        self.lb = None if lb is None else np.asarray(lb, dtype=np.float64)
 
     def W(self, r):
         return self.sig * w_q(r / self.h)
@@ -84,6 +101,12 @@ class Scene:
 
     def ddW(self, r):
         return self.sig / self.h ** 2 * ddw_q(r / self.h)
+
+    def C(self, r):
+        return self.csig * c_q(r / self.h)
+
+    def dC(self, r):
+        return self.csig / self.h * dc_q(r / self.h)
 
 
 # ----------------------------------------------------------------------------- topology
@@ -109,13 +132,34 @@ def pairs(x, y, h, same):
     return torch.as_tensor(ii[keep]), torch.as_tensor(jj[keep])
 
 
+def cell_candidates(x, lb, h):
+    """Directed fluid-fluid pairs (i, j), i != j, whose cells (``int((x - lb)
+    // h)`` in FP32, ``sph_util.py:65-67``) differ by at most one per axis: the
+    3^dim template's candidates of ``sph.py:156-160`` for particles away from
+    the grid's edges."""
+    f32 = np.float32
+    cell = np.floor((np.asarray(x, dtype=f32) - lb.astype(f32)) / f32(h)).astype(np.int64)
+    d = np.abs(cell[:, None, :] - cell[None, :, :]).max(axis=2)
+    ii, jj = np.nonzero(d <= 1)
+    keep = ii != jj
+    return torch.as_tensor(ii[keep]), torch.as_tensor(jj[keep])
+
+
 class Topology:
-    """Fluid-fluid pairs (directed, both ways) and fluid-boundary pairs of a substep."""
+    """Fluid-fluid pairs (directed, both ways) and fluid-boundary pairs of a
+    substep; with surface tension on, also the template candidates (ci, cj)."""
 
     def __init__(self, sc, x):
         xd = x.detach().cpu().numpy()
         self.fi, self.fj = pairs(xd, xd, sc.h, True)
         self.bi, self.bj = pairs(xd, sc.bpos.numpy(), sc.h, False)
+        if sc.gamma != 0.0:
+            if sc.lb is None:
+                raise ValueError("surface tension needs the grid origin (Scene lb)")
+            ci, cj = cell_candidates(xd, sc.lb, sc.h)
+            r = np.linalg.norm(xd[ci.numpy()] - xd[cj.numpy()], axis=1)
+            keep = torch.as_tensor(r > 0)
+            self.ci, self.cj = ci[keep], cj[keep]
 
 
 def _sum(idx, vals, n):
@@ -178,6 +222,30 @@ def viscosity_acc(sc, top, x, v, psi, mu):
     return sc.gravity[None, :] + mu * V
 
 
+def surface_tension_acc(sc, top, x, psi):
+    """SPH_advection_surface_tension_acc (sph.py:132-166), fluid-fluid, one
+    phase (volume fraction 1 everywhere): normals n_i = h sum_j -(X_j / psi_j)
+    g_ij r_ij, then a_i += sum_j 2 psi0_i / (psi_i + psi_j) (-gamma m_j C(r)
+    r_ij / r + gamma (n_i - n_j)).  The second sum runs over every template
+    candidate with r > 0, as the reference's loop does: the curvature term has
+    no kernel weight, so candidates beyond h contribute to it (C = 0 there).
+    Returns (acceleration, normals)."""
+    n = x.shape[0]
+    m = sc.mass
+    fi, fj = top.fi, top.fj
+    rf = x[fi] - x[fj]
+    r = rf.norm(dim=1)
+    g = sc.dW(r) / r
+    nrm = sc.h * _sum(fi, (-(m[fj] / psi[fj]) * g)[:, None] * rf, n)
+    ci, cj = top.ci, top.cj
+    rc = x[ci] - x[cj]
+    s = rc.norm(dim=1)
+    c = 2 * sc.rest_density[ci] / (psi[ci] + psi[cj])
+    coh = (-sc.gamma * m[cj] * sc.C(s) / s)[:, None] * rc
+    cur = sc.gamma * (nrm[ci] - nrm[cj])
+    return _sum(ci, c[:, None] * (coh + cur), n), nrm
+
+
 def solve(sc, top, x, u, psi, alpha, kind, compression, fixed_iters=None):
     """The loop of main.py:199-214 / 221-234 (iteration count recorded)."""
     it, comp = 0, compression
@@ -208,11 +276,16 @@ def substep(sc, x, v, mu, compression=0.0, top=None, iters=None, record=None):
     u, kd, compression, log_d = solve(sc, top, x, v, psi, alpha, 0, compression, None if iters is None else iters[0])
     vmid = u
     acc = viscosity_acc(sc, top, x, vmid, psi, mu)
+    nrm = None
+    if sc.gamma != 0.0:
+        st, nrm = surface_tension_acc(sc, top, x, psi)
+        acc = acc + st
     u = vmid + acc * sc.dt
     u, kp, compression, log_p = solve(sc, top, x, u, psi, alpha, 1, compression, None if iters is None else iters[1])
     x2 = x + u * sc.dt
     if record is not None:
-        record.update(top=top, rho=rho, alpha=alpha, a1=a1, a2=a2, vmid=vmid, log_d=log_d, log_p=log_p, x=x)
+        record.update(top=top, rho=rho, alpha=alpha, a1=a1, a2=a2, vmid=vmid, log_d=log_d, log_p=log_p, x=x,
+                      nrm=nrm)
     return x2, u, compression, (kd, kp)
 
 
@@ -314,6 +387,51 @@ def adjoint_viscosity(sc, top, x, v, psi, mu, lam_a, lam_x, lam_psi):
     return lam_v, gmu
 
 
+def adjoint_surface_tension(sc, top, x, psi, nrm, lam_a, lam_x, lam_psi):
+    """Reverse of :func:`surface_tension_acc` in two gather sweeps: adds into
+    lam_x and lam_psi.  With c_ij = 2 psi0_i / (psi_i + psi_j) and B_ij =
+    -gamma m_j C(r) r_ij / r + gamma (n_i - n_j), a_i = sum_j c_ij B_ij, so
+
+      lam_n_i    = gamma sum_j (c_ij lam_a_i - c_ji lam_a_j),
+      lam_psi_i -= sum_j (c_ij lam_a_i.B_ij + c_ji lam_a_j.B_ji) / (psi_i + psi_j),
+      lam_x_i   += sum_j (k_ij D_C(lam_a_i) - k_ji D_C(lam_a_j)),  k_ij = -gamma m_j c_ij,
+      D_C(w) = (C/r) w + ((C' - C/r) / r^2)(r_ij.w) r_ij (the cohesion's pair term);
+
+    then the normals' reverse, sweep 2:
+
+      lam_x_i   += h sum_j ((m_i / psi_i) D(lam_n_j) - (m_j / psi_j) D(lam_n_i)),
+      lam_psi_i -= h (m_i / psi_i^2) sum_j g_ij r_ij.lam_n_j,
+
+    D the pair gradient's derivative of :func:`_dgrad`."""
+    n = x.shape[0]
+    m = sc.mass
+    gam = sc.gamma
+    # sweep 1, over the template candidates: lam_n, the psi terms of c, the
+    # cohesion's position terms
+    ci, cj = top.ci, top.cj
+    rc, s_, s2, _, _, _ = _pair_geom(sc, x[ci], x[cj])
+    gC = sc.C(s_) / s_
+    G2C = (sc.dC(s_) - gC) / s2
+    s = psi[ci] + psi[cj]
+    cij = 2 * sc.rest_density[ci] / s
+    cji = 2 * sc.rest_density[cj] / s
+    dn = nrm[ci] - nrm[cj]
+    Bij = (-gam * m[cj] * gC)[:, None] * rc + gam * dn
+    Bji = (gam * m[ci] * gC)[:, None] * rc - gam * dn
+    la_i, la_j = lam_a[ci], lam_a[cj]
+    lam_n = gam * _sum(ci, cij[:, None] * la_i - cji[:, None] * la_j, n)
+    lam_psi -= _sum(ci, (cij * (la_i * Bij).sum(1) + cji * (la_j * Bji).sum(1)) / s, n)
+    kij, kji = -gam * m[cj] * cij, -gam * m[ci] * cji
+    lam_x += _sum(ci, kij[:, None] * _dgrad(gC, G2C, rc, la_i) - kji[:, None] * _dgrad(gC, G2C, rc, la_j), n)
+    # sweep 2, over the pairs within h: the normals' reverse
+    fi, fj = top.fi, top.fj
+    rv, r, r2, g, G2, _ = _pair_geom(sc, x[fi], x[fj])
+    ln_i, ln_j = lam_n[fi], lam_n[fj]
+    lam_x += sc.h * _sum(fi, (m[fi] / psi[fi])[:, None] * _dgrad(g, G2, rv, ln_j)
+                         - (m[fj] / psi[fj])[:, None] * _dgrad(g, G2, rv, ln_i), n)
+    lam_psi -= sc.h * m / psi ** 2 * _sum(fi, g * (rv * ln_j).sum(1), n)
+
+
 def adjoint_density_alpha(sc, top, x, a1, a2, lam_psi, lam_alpha, lam_x):
     """Reverse of density + alpha (sph.py:50-105): adds the position terms into lam_x."""
     n = x.shape[0]
@@ -347,6 +465,8 @@ def adjoint_substep(sc, rec, mu, lam_x2, lam_v2):
         lam_u = adjoint_iteration(sc, top, x, u, kap, s, alpha, lam_u, lam_x, lam_psi, lam_alpha)
     lam_a = lam_u * dt
     lam_vv, gmu = adjoint_viscosity(sc, top, x, rec["vmid"], psi, mu, lam_a, lam_x, lam_psi)
+    if sc.gamma != 0.0:
+        adjoint_surface_tension(sc, top, x, psi, rec["nrm"], lam_a, lam_x, lam_psi)
     lam_u = lam_u + lam_vv
     for (u, kap, s) in reversed(rec["log_d"]):
         lam_u = adjoint_iteration(sc, top, x, u, kap, s, alpha, lam_u, lam_x, lam_psi, lam_alpha)

@@ -13,11 +13,11 @@ from oracle import sph_autodiff as A
 from oracle import sph_oracle as O
 
 
-def small_scene(nx=6, ny=6, nz=6, fixed_iters=2, relax=1.0):
+def small_scene(nx=6, ny=6, nz=6, fixed_iters=2, relax=1.0, gamma=0.0):
     """The differentiable workload at a small size, as (params, numpy sets, autodiff scene, x0, v0, target)."""
     from tichi_sph_gb300 import sph_config, workloads
     from tichi_sph_gb300.simulation import Simulation
-    c, s, vel, target = workloads.diff_block(nx=nx, ny=ny, nz=nz, fixed_iters=fixed_iters, relax=relax)
+    c, s, vel, target = workloads.diff_block(nx=nx, ny=ny, nz=nz, fixed_iters=fixed_iters, relax=relax, gamma=gamma)
     cfg = sph_config.Config(c, s)
     sim = Simulation(cfg, device="cpu")
     sim.init_scenario()
@@ -30,12 +30,16 @@ def small_scene(nx=6, ny=6, nz=6, fixed_iters=2, relax=1.0):
     dt = float(np.float32(np.float32(p.part_size) / np.float32(p.cs)))
     sc = A.Scene(3, p.h, p.sig, fa["mass"], fa["rest_density"], ba["pos"], ba["mass"], p.gravity, dt,
                  iters=(p.iter_min, p.iter_min), tol=(p.divergence_threshold, p.compression_threshold),
-                 iter_max=p.iter_max)
+                 iter_max=p.iter_max, gamma=p.surface_tension_gamma, lb=p.lb)
     return p, fa, ba, sc, torch.as_tensor(fa["pos"]), torch.as_tensor(fa["vel"]), torch.as_tensor(target)
 
 
-def test_forward_matches_numpy_oracle():
-    p, fa, ba, sc, x0, v0, _ = small_scene(fixed_iters=None)
+GAMMAS = [0.0, 0.07]   # without and with surface tension (the coefficient of the two-phase workload)
+
+
+@pytest.mark.parametrize("gamma", GAMMAS)
+def test_forward_matches_numpy_oracle(gamma):
+    p, fa, ba, sc, x0, v0, _ = small_scene(fixed_iters=None, gamma=gamma)
     fluid, bound = O.sets_from_arrays(p, fa, ba)
     st = O.Stats()
     O.run_substep(fluid, bound, p, st)
@@ -71,8 +75,9 @@ def _autograd(sc, x0, v0, mu, target, steps):
     return v.grad, m.grad
 
 
-def test_autograd_matches_central_differences():
-    _, _, _, sc, x0, v0, target = small_scene()
+@pytest.mark.parametrize("gamma", GAMMAS)
+def test_autograd_matches_central_differences(gamma):
+    _, _, _, sc, x0, v0, target = small_scene(gamma=gamma)
     mu = torch.tensor(0.01, dtype=A.T)
     steps = 3
     gv, gmu = _autograd(sc, x0, v0, mu, target, steps)
@@ -85,8 +90,9 @@ def test_autograd_matches_central_differences():
     assert abs(float(fd_v) - float((gv * d).sum())) <= 1e-5 * abs(float(fd_v))
 
 
-def test_hand_adjoint_matches_autograd():
-    _, _, _, sc, x0, v0, target = small_scene()
+@pytest.mark.parametrize("gamma", GAMMAS)
+def test_hand_adjoint_matches_autograd(gamma):
+    _, _, _, sc, x0, v0, target = small_scene(gamma=gamma)
     mu = torch.tensor(0.01, dtype=A.T)
     steps = 3
     gv_ref, gmu_ref = _autograd(sc, x0, v0, mu, target, steps)

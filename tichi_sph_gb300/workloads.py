@@ -142,7 +142,7 @@ def batched_dambreaks(n_scenes=256, seed=4, spacing=0.01, n_min=2000, n_max=2000
     return out
 
 
-def diff_block(nx=46, ny=46, nz=47, spacing=0.01, seed=5, v_std=0.1, fixed_iters=None, relax=1.0):
+def diff_block(nx=46, ny=46, nz=47, spacing=0.01, seed=5, v_std=0.1, fixed_iters=None, relax=1.0, gamma=0.0):
     """Differentiable DFSPH scene: a block of nx*ny*nz fluid particles (46 x 46 x 47
     = 99,452 by default) in the x/z-min corner of a tank 1.6 x 1.5 x 1.6 block
     lengths with 3 boundary layers, dt = 5e-4 (``solver_cs`` 20; the CFL limit
@@ -151,7 +151,8 @@ def diff_block(nx=46, ny=46, nz=47, spacing=0.01, seed=5, v_std=0.1, fixed_iters
     (config, scenario, initial-velocity function, target point); ``relax`` < 1
     emits the same lattice at relax x spacing (a compressed block).  Velocities are
     seeded N(0, v_std) per component, the target is the block's centre plus a
-    seeded U(-0.05, 0.05) offset per axis."""
+    seeded U(-0.05, 0.05) offset per axis; ``gamma`` is the surface-tension
+    coefficient."""
     import numpy as np
     Lx, Ly, Lz = nx * spacing, ny * spacing, nz * spacing
     t = 3.5 * spacing
@@ -161,10 +162,10 @@ def diff_block(nx=46, ny=46, nz=47, spacing=0.01, seed=5, v_std=0.1, fixed_iters
     shape = ((np.array(box_hi, np.float32) - np.array(box_lo, np.float32) + 1e-7) / sp32).astype(np.int32)
     n_box = int(np.prod(shape.astype(np.int64)) - np.prod(np.maximum(shape.astype(np.int64) - 6, 0)))
     if fixed_iters:
-        cfg = _config(cs=20, div_tol=1e9, comp_tol=1e9)
+        cfg = _config(cs=20, div_tol=1e9, comp_tol=1e9, gamma=gamma)
         cfg["solver_iter_threshold_min"] = int(fixed_iters)
     else:
-        cfg = _config(cs=20)
+        cfg = _config(cs=20, gamma=gamma)
     scen = {
         "sim_env": {"global_part_size": spacing, "global_dynamic_viscosity": 0.01, "sim_dim": 3,
                     "sim_space_lb": [b - 0.1 for b in box_lo],
