@@ -20,6 +20,8 @@
 //     k_adj_vel:   lam_u = lam_u' + dt sum_j (lam_s_i X_j + lam_s_j X_i) g r_ij,
 //                  lam_x += d/dx of the divergence's pair terms;
 //   k_adj_visc reverses a = g + mu V(x, v, psi) (and yields dL/dmu);
+//   k_adj_st1 / k_adj_st2 reverse the surface tension (sph.py:132-166): its
+//     cohesion and curvature over the template candidates, then the normals;
 //   k_adj_density reverses the density and alpha sums.
 // The position derivative of a pair term g(r) r_ij . w is g w + (g'(r)/r)(r_ij . w) r_ij
 // with g'(r)/r = (W''(r) - g(r)) / r^2.  Each pair appears in both particles'
@@ -48,6 +50,14 @@ __device__ __forceinline__ float kwgg(float q) {
     return q <= 0.5f ? 6.f * (6.f * q - 2.f) : (q < 1.f ? 12.f * (1.f - q) : 0.f);
 }
 
+// Derivative of the cohesion spline shape kcoh: 3 q^2 (1 - q)^2 (1 - 2 q),
+// doubled below q = 1/2.
+__device__ __forceinline__ float kcohd(float q) {
+    const float b = 1.f - q;
+    const float t = 3.f * q * q * b * b * (1.f - 2.f * q);
+    return q <= 0.5f ? 2.f * t : (q < 1.f ? t : 0.f);
+}
+
 // ----------------------------------------------------------------------------- recording
 __global__ void k_tape_begin(TapeArrays a, int slot) {
     *a.dslot = slot;
@@ -70,6 +80,7 @@ __global__ void __launch_bounds__(kBlock) k_tape_state(KConst k, FluidBuf F, Bou
         a.a1[o] = F.a1[s];
         a.a2[o] = F.dens[s].w;
         a.rho0[o] = F.rho0[s];
+        if (a.vf0) a.vf0[o] = F.vf[s];
         const unsigned int pc = F.nbr_cnt[s];
         a.cnt[o] = pc;
         if (pc == kNbrOverflow) {
@@ -119,6 +130,14 @@ __global__ void __launch_bounds__(kBlock) k_tape_vmid(KConst k, FluidBuf F, Tape
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (s >= k.s0.f_n) return;
     a.vmid[*a.dslot * a.cap + s] = F.vel[s];
+    if (a.nrm) a.nrm[*a.dslot * a.cap + s] = F.normal[s];
+}
+
+// The fluid grid's cell starts of the recorded substep (surface tension on: its
+// reverse visits the same template candidates as the forward).
+__global__ void __launch_bounds__(kBlock) k_tape_start(FluidBuf F, TapeArrays a) {
+    const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (i < a.nstart) a.start[(int64_t)(*a.dslot) * a.nstart + i] = F.start[i];
 }
 
 __global__ void k_tape_end(KConst k, TapeArrays a) {
@@ -143,9 +162,13 @@ struct SlotView {
     const int *nbr;
     const float4 *u;     // [2][max_iters][cap]
     const float *kap;
+    const float4 *nrm;   // surface tension on: normals, phase-0 volume fractions, cell starts
+    const float *vf0;
+    const int *start;
+    Geo geo;
     int64_t cap;
     int n, max_iters;
-    float dt, mu, h2, inv_h, sig_h, eps;
+    float dt, mu, h, h2, inv_h, sig_h, eps, gamma, c_coh;
 };
 
 // Pair geometry of r_ij = pi - pj (0 < r < h): g = W'(r)/r, G2 = g'(r)/r, W2 = W''(r).
@@ -338,6 +361,99 @@ __global__ void __launch_bounds__(kBlock) k_adj_visc(SlotView v, const float4 *_
     }
 }
 
+// Surface tension, first reverse sweep, over the template candidates the
+// forward visits (sph.py:156-166).  With c_ij = 2 psi0_i / (psi_i + psi_j),
+// B_ij = -gamma m_j C(r) r_ij / r + gamma (n_i - n_j) and lam_a = dt lam_u:
+//   lam_n_i    = gamma sum_j (c_ij lam_a_i - c_ji lam_a_j),
+//   lam_psi_i -= sum_j (c_ij lam_a_i.B_ij + c_ji lam_a_j.B_ji) / (psi_i + psi_j),
+//   lam_x_i   += sum_j (k_ij D_C(lam_a_i) - k_ji D_C(lam_a_j)), k_ij = -gamma m_j c_ij,
+// D_C(w) = (C/r) w + ((C' - C/r) / r^2)(r_ij.w) r_ij.  Pairs count only where
+// both particles' phase-0 volume fraction exceeds 0.99, as in the forward.
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_adj_st1(SlotView v, const float4 *__restrict__ lu, float4 *ln,
+                                                    float4 *lx, float *lpsi) {
+    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (s >= v.n) return;
+    const float4 pi = v.pos[s];
+    const float4 mpi = v.mpsi[s];
+    const float mi = mpi.x, psii = mpi.y, r0i = mpi.z;
+    const float4 ni = v.nrm[s];
+    const float4 lui = lu[s];
+    const float lax = v.dt * lui.x, lay = v.dt * lui.y, laz = v.dt * lui.z;
+    const float gam = v.gamma;
+    float nx = 0.f, ny = 0.f, nz = 0.f, lp = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+    bool ok;
+    const long long code = cell_code<DIM>(pi, v.geo, ok);
+    if (ok && v.vf0[s] > 0.99f) {
+        visit_candidates<DIM>(v.start, v.geo, code, 0, 0, [&](int j) {
+            const float4 pj = v.pos[j];
+            const float x = pi.x - pj.x, y = pi.y - pj.y, z = pi.z - pj.z;
+            const float r2 = x * x + y * y + z * z;
+            if (!(r2 > 0.f) || !(v.vf0[j] > 0.99f)) return;
+            float r;
+            const float ri = pair_rinv(r2, r);
+            const float q = r * v.inv_h;
+            const float gC = kcoh(q) * v.c_coh * ri;
+            const float G2C = (kcohd(q) * v.c_coh * v.inv_h - gC) * (ri * ri);
+            const float4 mpj = v.mpsi[j];
+            const float mj = mpj.x, psij = mpj.y, r0j = mpj.z;
+            const float4 nj = v.nrm[j];
+            const float4 luj = lu[j];
+            const float ljx = v.dt * luj.x, ljy = v.dt * luj.y, ljz = v.dt * luj.z;
+            const float sum = psii + psij;
+            const float cij = 2.f * r0i / sum, cji = 2.f * r0j / sum;
+            const float dnx = ni.x - nj.x, dny = ni.y - nj.y, dnz = ni.z - nj.z;
+            const float rli = x * lax + y * lay + z * laz, rlj = x * ljx + y * ljy + z * ljz;
+            const float laBij = -gam * mj * gC * rli + gam * (dnx * lax + dny * lay + dnz * laz);
+            const float laBji = gam * mi * gC * rlj - gam * (dnx * ljx + dny * ljy + dnz * ljz);
+            nx += gam * (cij * lax - cji * ljx);
+            ny += gam * (cij * lay - cji * ljy);
+            nz += gam * (cij * laz - cji * ljz);
+            lp -= (cij * laBij + cji * laBji) / sum;
+            const float kij = -gam * mj * cij, kji = -gam * mi * cji;
+            gx += kij * (gC * lax + G2C * rli * x) - kji * (gC * ljx + G2C * rlj * x);
+            gy += kij * (gC * lay + G2C * rli * y) - kji * (gC * ljy + G2C * rlj * y);
+            gz += kij * (gC * laz + G2C * rli * z) - kji * (gC * ljz + G2C * rlj * z);
+        });
+    }
+    ln[s] = make_float4(nx, ny, nz, 0.f);
+    const float4 o = lx[s];
+    lx[s] = make_float4(o.x + gx, o.y + gy, o.z + gz, 0.f);
+    lpsi[s] += lp;
+}
+
+// Surface tension, second reverse sweep: the normals n_i = h sum_j -(X_j /
+// psi_j) g_ij r_ij over the pairs within h,
+//   lam_x_i   += h sum_j ((X_i / psi_i) D(lam_n_j) - (X_j / psi_j) D(lam_n_i)),
+//   lam_psi_i -= h (X_i / psi_i^2) sum_j g_ij r_ij.lam_n_j,
+// D(w) = g w + G2 (r_ij.w) r_ij.
+__global__ void __launch_bounds__(kBlock) k_adj_st2(SlotView v, const float4 *__restrict__ ln, float4 *lx,
+                                                    float *lpsi) {
+    const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (s >= v.n) return;
+    const float4 pi = v.pos[s];
+    const float psii = v.mpsi[s].y;
+    const float ai = pi.w / psii;
+    const float4 ni = ln[s];
+    float gx = 0.f, gy = 0.f, gz = 0.f, lp = 0.f;
+    for_pairs(v, s,
+        [&](int j) {
+            const float4 pj = v.pos[j];
+            const Pair P(v, pi, pj);
+            const float aj = pj.w / v.mpsi[j].y;
+            const float4 nj = ln[j];
+            const float rj = P.dot(nj.x, nj.y, nj.z), rI = P.dot(ni.x, ni.y, ni.z);
+            gx += ai * (P.g * nj.x + P.G2 * rj * P.x) - aj * (P.g * ni.x + P.G2 * rI * P.x);
+            gy += ai * (P.g * nj.y + P.G2 * rj * P.y) - aj * (P.g * ni.y + P.G2 * rI * P.y);
+            gz += ai * (P.g * nj.z + P.G2 * rj * P.z) - aj * (P.g * ni.z + P.G2 * rI * P.z);
+            lp += P.g * rj;
+        },
+        [&](int) {});
+    const float4 o = lx[s];
+    lx[s] = make_float4(o.x + v.h * gx, o.y + v.h * gy, o.z + v.h * gz, 0.f);
+    lpsi[s] -= v.h * ai / psii * lp;
+}
+
 // lam of alpha's two sums: (lam_alpha1 xyz, lam_alpha2) where alpha was not clamped.
 __global__ void __launch_bounds__(kBlock) k_adj_alpha_prep(SlotView v, const float *__restrict__ lalpha, float4 *la1) {
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
@@ -444,10 +560,29 @@ SlotView slot_view(const tsph_tape &t, int slot) {
     v.max_iters = a.max_iters;
     v.dt = m.dt;
     v.mu = m.mu;
+    v.h = c.h;
     v.h2 = c.h2;
     v.inv_h = c.inv_h;
     v.sig_h = c.sig_h;
     v.eps = 0.01f * c.h2;
+    v.gamma = a.nrm ? c.gamma : 0.f;
+    v.c_coh = c.c_coh;
+    v.nrm = a.nrm ? a.nrm + o : nullptr;
+    v.vf0 = a.vf0 ? a.vf0 + o : nullptr;
+    v.start = a.start ? a.start + (int64_t)slot * a.nstart : nullptr;
+    Geo &g = v.geo;
+    for (int d = 0; d < 3; ++d) g.lb[d] = c.lb[d];
+    g.h = c.h;
+    g.h2 = c.h2;
+    g.inv_h = c.inv_h;
+    g.sig = c.sig;
+    g.sig_h = c.sig_h;
+    g.node_num = c.node_num;
+    g.nx = c.nx;
+    g.nxny = c.nxny;
+    g.cbase = c.cbase;
+    g.R = t.ctx->k.R;
+    g.row_trim = c.row_trim;
     return v;
 }
 
@@ -484,6 +619,11 @@ void launch_tape_state(tsph_ctx &c, cudaStream_t st) {
     const int64_t n = c.F.cap > c.B.cap ? c.F.cap : c.B.cap;
     c.launches += 1;
     k_tape_state<<<blocks_for(n), kBlock, 0, st>>>(c.k, c.F, c.B, c.rec_tape->a);
+    const TapeArrays &a = c.rec_tape->a;
+    if (a.start) {
+        c.launches += 1;
+        k_tape_start<<<blocks_for(a.nstart), kBlock, 0, st>>>(c.F, a);
+    }
 }
 
 void launch_tape_iter(tsph_ctx &c, int kind, cudaStream_t st) {
@@ -522,8 +662,8 @@ int tsph_tape_create(tsph_ctx *c, int slots, int max_iters, tsph_tape **out) {
     if (!c || !out || slots < 1 || max_iters < 1) return fail_text(TSPH_ERR_INVALID, "bad argument");
     *out = nullptr;
     if (c->n_scenes != 1 || c->batch) return fail_text(TSPH_ERR_INVALID, "the adjoint supports one-scene contexts");
-    if (c->p.solver_type != TSPH_DFSPH || c->p.fbm_enabled || c->p.surface_tension_gamma != 0.f)
-        return fail_text(TSPH_ERR_INVALID, "the adjoint supports DFSPH without surface tension or FBM");
+    if (c->p.solver_type != TSPH_DFSPH || c->p.fbm_enabled)
+        return fail_text(TSPH_ERR_INVALID, "the adjoint supports DFSPH without the volume-fraction update");
     tsph_tape *t = new (std::nothrow) tsph_tape();
     if (!t) return fail_text(TSPH_ERR_INVALID, "out of host memory");
     t->ctx = c;
@@ -568,6 +708,13 @@ int tsph_tape_create(tsph_ctx *c, int slots, int max_iters, tsph_tape **out) {
     t->lam_alpha = (float *)get(N * sizeof(float));
     t->partials = (double *)get((N / kBlock + 2) * sizeof(double));
     t->ticket = (unsigned int *)get(sizeof(unsigned int));
+    if (c->st_on) {
+        a.nstart = c->k.total_nodes + 1;
+        a.nrm = (float4 *)get(S * N * sizeof(float4));
+        a.vf0 = (float *)get(S * N * sizeof(float));
+        a.start = (int *)get(S * (size_t)a.nstart * sizeof(int));
+        t->lam_n = (float4 *)get(N * sizeof(float4));
+    }
     if (err == cudaSuccess) err = cudaMallocHost((void **)&t->host_meta, S * sizeof(TapeMeta));
     if (err == cudaSuccess) err = cudaDeviceSynchronize();
     if (err != cudaSuccess) {
@@ -612,6 +759,12 @@ int tsph_substep_adjoint(tsph_ctx *c, tsph_tape *t, int slot, const float *gx_ou
     }
     if (dim == 3) k_adj_visc<3><<<nb, kBlock, 0, st>>>(v, lu, lu2, t->lam_x, t->lam_psi, t->partials, t->ticket, gmu);
     else k_adj_visc<2><<<nb, kBlock, 0, st>>>(v, lu, lu2, t->lam_x, t->lam_psi, t->partials, t->ticket, gmu);
+    if (v.gamma != 0.f) {
+        // the surface tension's reverse reads the same lam_a = dt lam_u as k_adj_visc
+        if (dim == 3) k_adj_st1<3><<<nb, kBlock, 0, st>>>(v, lu, t->lam_n, t->lam_x, t->lam_psi);
+        else k_adj_st1<2><<<nb, kBlock, 0, st>>>(v, lu, t->lam_n, t->lam_x, t->lam_psi);
+        k_adj_st2<<<nb, kBlock, 0, st>>>(v, t->lam_n, t->lam_x, t->lam_psi);
+    }
     float4 *tmp = lu;
     lu = lu2;
     lu2 = tmp;

@@ -29,6 +29,12 @@ struct TapeArrays {
     int *nbr;
     TapeMeta *meta;
     int *dslot;  // slot being recorded (set before a recorded step, read by its kernels)
+    // with surface tension on: the normals, phase 0's volume fraction and the
+    // fluid grid's cell starts (nstart per slot) of each recorded substep
+    float4 *nrm;
+    float *vf0;
+    int *start;
+    int64_t nstart;
     int64_t cap, bcap;
     int slots, max_iters, nbr_max;
 };
@@ -42,6 +48,7 @@ struct tsph_tape {
     int host_valid;             // host_meta matches the device
     // reverse-pass scratch in sorted order (cap entries)
     float4 *lam_u, *lam_u2, *lam_x, *lam_a1;
+    float4 *lam_n;  // adjoint of the surface normals (surface tension on)
     float *lam_s, *lam_psi, *lam_alpha;
     double *partials;
     unsigned int *ticket;
