@@ -247,18 +247,19 @@ int tsph_map_velocity(tsph_ctx *ctx, const tsph_set *fluid, const float *lb, flo
  * Hand-written reverse mode of the substep (no counterpart in the reference,
  * which has no autodiff; the forward it reverses is tsph_substep, i.e. the
  * substep of main.py:347-352 around sph_step, main.py:175-256).  Supported for
- * a single-scene DFSPH context without surface tension or volume-fraction
- * update.  Differentiable inputs: fluid positions and velocities at the start
+ * a single-scene DFSPH context (viscosity and surface tension; not the
+ * volume-fraction update).  Differentiable inputs: fluid positions and velocities at the start
  * of the substep and the dynamic viscosity.  Held fixed: masses, rest
  * densities, the boundary, dt, the iteration counts of the two Jacobi solves
- * (those the forward took) and the neighbour pairs of the substep (the
- * topology found at its start).  The clamps psi_adv = max(., 0) and
+ * (those the forward took) and the neighbour pairs and template candidates of
+ * the substep (the topology found at its start).  The clamps psi_adv = max(., 0) and
  * alpha = max(., 1e-4) are differentiated one-sided.
  *
  * A tape holds `slots` recorded substeps (or density evaluations) with at most
  * `max_iters` iterations per Jacobi solve.  Recording writes what the reverse
  * sweeps need -- the sorted order, positions, neighbour lists, density and
- * alpha terms, every Jacobi iterate -- into device memory owned by the tape;
+ * alpha terms, every Jacobi iterate, and with surface tension the normals and
+ * cell starts -- into device memory owned by the tape;
  * the reverse pass reads only the tape.  The caller arranges checkpointing. */
 typedef struct tsph_tape tsph_tape;
 
