@@ -374,17 +374,18 @@ def other_line(res, args, ws):
                        "min_volume_fraction": res["vf_min"]}}
 
 
-def run_adjoint(reps, warmup, dev, substeps=64, checkpoint_every=8):
+def run_adjoint(reps, warmup, dev, substeps=64, checkpoint_every=8, gamma=0.0):
     """Config of the differentiable form: a 99,452-particle block, 64 substeps at
     dt 5e-4, loss = |centre of mass - target|^2 + 0.1 mean density error^2,
     gradients with respect to the initial velocities and the viscosity.  Times
     the forward (rollout + final density) and the backward (recompute of every
-    checkpoint segment but the last + the reverse sweeps) with CUDA events."""
+    checkpoint segment but the last + the reverse sweeps) with CUDA events.
+    ``gamma`` != 0 adds surface tension (forward and reverse)."""
     import torch
     from tichi_sph_gb300 import sph_config, workloads
     from tichi_sph_gb300.adjoint import DiffRollout, com_density_loss
     from tichi_sph_gb300.simulation import Simulation
-    c, sc_, vel, target = workloads.diff_block()
+    c, sc_, vel, target = workloads.diff_block(gamma=gamma)
     cfg = sph_config.Config(c, sc_)
     sim = Simulation(cfg, device=dev)
     sim.init_scenario()
@@ -418,7 +419,7 @@ def run_adjoint(reps, warmup, dev, substeps=64, checkpoint_every=8):
     return {"n": n, "nb": sim.bound.part_num[None], "substeps": substeps, "checkpoint_every": checkpoint_every,
             "forward_ms": fwm, "backward_ms": bwm, "ratio": bwm / fwm, "grad_v_norm": gnorm, "grad_mu": gmu,
             "loss": loss, "reps": reps, "warmup": warmup, "last_div_iter": st["div_iter"],
-            "last_incom_iter": st["incom_iter"]}
+            "last_incom_iter": st["incom_iter"], "gamma": gamma}
 
 
 def adjoint_line(res, args, ws):
@@ -427,8 +428,9 @@ def adjoint_line(res, args, ws):
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "differentiable DFSPH: %d-particle block (46 x 46 x 47 at 0.01 m) in a 3-layer "
                                    "tank (%d boundary), %d substeps at dt 5e-4, checkpoint every %d; loss |CoM - "
-                                   "target|^2 + 0.1 mean((rho - rho0) / rho0)^2; d/d(initial velocities), d/d(mu)"
-                                   % (res["n"], res["nb"], res["substeps"], res["checkpoint_every"]),
+                                   "target|^2 + 0.1 mean((rho - rho0) / rho0)^2; d/d(initial velocities), d/d(mu)%s"
+                                   % (res["n"], res["nb"], res["substeps"], res["checkpoint_every"],
+                                      "; surface tension %g" % res["gamma"] if res["gamma"] else ""),
                        "forward_ms": res["forward_ms"], "backward_ms": res["backward_ms"],
                        "forward_particle_steps_per_s": res["n"] * res["substeps"] / (res["forward_ms"] / 1e3),
                        "loss": res["loss"], "grad_v_norm": res["grad_v_norm"], "grad_mu": res["grad_mu"],
@@ -464,6 +466,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-side", type=int, default=100)
+    ap.add_argument("--gamma", type=float, default=0.0,
+                    help="surface-tension coefficient of the adjoint workload (0: none)")
     ap.add_argument("--spacing", type=float, default=0.01,
                     help="particle spacing of the 3D dam break (the cube is n-side particles wide, the tank fixed)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -502,7 +506,7 @@ def main():
             dist.destroy_process_group()
         return 0
     if args.workload == "adjoint":
-        res = run_adjoint(args.steps, args.warmup, dev)
+        res = run_adjoint(args.steps, args.warmup, dev, gamma=args.gamma)
         if rank == 0:
             print(json.dumps(adjoint_line(res, args, ws)), flush=True)
         if dist:
