@@ -148,3 +148,20 @@ def test_hand_adjoint_clamps(clamped):
         gmu += g
     assert float((gv - gv_ref).norm()) <= 1e-10 * float(gv_ref.norm())
     assert abs(gmu - float(gmu_ref)) <= 1e-10 * abs(float(gmu_ref))
+
+
+def test_cell_candidates_equal_the_reference_template():
+    """The surface tension's candidate pairs of the autodiff oracle (cells at
+    most one apart per axis) are exactly the numpy oracle's template candidates
+    (sph.py:156-160 over the reference's linear cell codes), self pairs aside,
+    and they hold every pair within h."""
+    p, fa, ba, sc, x0, _, _ = small_scene(gamma=0.07)
+    fluid, bound = O.sets_from_arrays(p, fa, ba)
+    grid = O.Grid(p, [fluid, bound])
+    pr = grid.pairs(fluid, fluid)
+    ref = {(int(i), int(j)) for i, j in zip(pr.i, pr.j) if i != j}
+    ci, cj = A.cell_candidates(fa["pos"], p.lb, p.h)
+    got = set(zip(ci.tolist(), cj.tolist()))
+    assert got == ref
+    fi, fj = A.pairs(fa["pos"], fa["pos"], p.h, True)
+    assert set(zip(fi.tolist(), fj.tolist())) <= got
