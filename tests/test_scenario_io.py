@@ -1,7 +1,8 @@
 """Host side of run-time scenario emission and per-frame output (CPU, no
 stepping): inlets and delayed objects (main.py:26-112, sph_obj.py:117-137),
 the PLY writer (sph_util.py:90-100) and the files of one frame (main.py:371-378,
-the frame JSON of main.py:151-171)."""
+the frame JSON of main.py:151-171), written at once or by the background
+writer."""
 import json
 import os
 
@@ -127,3 +128,34 @@ def test_frame_files(tmp_path):
     assert set(rec["energy"]) == {"statistics_kinetic_energy", "statistics_gravity_potential_energy", "sum_energy"}
     assert rec["frame"] == 3
     assert sorted(os.listdir(out)) == ["json", "part_data", "ply"]
+
+
+def test_frames_written_in_the_background(tmp_path):
+    """write_files(wait=False): each frame's files hold the state at the call,
+    although the state changes before the background writes finish; flush waits
+    for all of them."""
+    import torch
+    sim = _sim(tmp_path, [_cube([0.0, 0.0, 0.0], [0.1, 0.1, 0.1])])
+    n = sim.fluid.part_num[None]
+    want = {}
+    for frame in range(1, 6):
+        sim.globalvar.time_counter = frame
+        sim.fluid.pos[:n] += torch.tensor([0.01, 0.0, 0.0])
+        want[frame] = sim.fluid.pos[:n].numpy().copy()
+        sim.write_files(wait=False)
+    sim.flush()
+    out = tmp_path / "out"
+    for frame, pos in want.items():
+        np.testing.assert_array_equal(np.load(out / "part_data" / ("pos_%d.npy" % frame)), pos)
+        assert json.loads((out / "json" / ("frame%d.json" % frame)).read_text())["frame"] == frame
+
+
+def test_background_write_error_surfaces_at_flush(tmp_path):
+    sim = _sim(tmp_path, [_cube([0.0, 0.0, 0.0], [0.1, 0.1, 0.1])])
+    blocker = tmp_path / "blocked"
+    blocker.write_text("a file where the output folder should be")
+    sim.out_dir = str(blocker)
+    sim.write_files(wait=False)
+    with pytest.raises(OSError):
+        sim.flush()
+    sim.flush()  # the error is reported once

@@ -30,7 +30,8 @@ def main(argv=None):
     while sim.globalvar.time_count < a.until:
         sim.run_step(verbose=True)
         if a.write:
-            sim.write_files()
+            sim.write_files(wait=False)  # files written in the background while stepping on
+    sim.flush()
     return 0
 
 

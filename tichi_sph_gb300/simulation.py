@@ -8,6 +8,8 @@ by ``time``), ``run_step`` (``main.py:339-368``) and the output writers
 """
 import json
 import os
+import queue
+import threading
 import time
 import warnings
 
@@ -64,6 +66,41 @@ def write_ply(path, frame_num, dim, num, pos):
             f.write("%s %s %s\n" % (np.float32(pos[i, 0]), np.float32(pos[i, 1]), np.float32(z)))
 
 
+class FrameWriter:
+    """Writes frames' files in submission order on one background thread, so
+    that the time loop goes on while a frame's PLY / JSON / npy files are
+    written.  ``flush`` waits for every submitted frame and re-raises the first
+    error a write met."""
+
+    def __init__(self):
+        self._q = queue.Queue()
+        self._thread = None
+        self._err = None
+
+    def submit(self, job):
+        if self._thread is None:
+            self._thread = threading.Thread(target=self._run, name="frame-writer", daemon=True)
+            self._thread.start()
+        self._q.put(job)
+
+    def _run(self):
+        while True:
+            job = self._q.get()
+            try:
+                job()
+            except BaseException as e:  # reported by flush
+                if self._err is None:
+                    self._err = e
+            finally:
+                self._q.task_done()
+
+    def flush(self):
+        self._q.join()
+        if self._err is not None:
+            err, self._err = self._err, None
+            raise err
+
+
 class Simulation:
     """The reference's module-level state of ``main.py`` as one object."""
 
@@ -82,6 +119,7 @@ class Simulation:
         self.grid = Grid(config, device=device) if map_grid else None
         self.out_dir = out_dir or config.solver_type
         self._solver = None
+        self._writer = None
 
     @property
     def solver(self):
@@ -231,18 +269,38 @@ class Simulation:
                        "sum_energy": ke + pe},
         }
 
-    def write_files(self):
+    def write_files(self, wait=True):
         """``main.py:371-378`` without the PNG: PLY of fluid positions, frame JSON,
-        npy of positions and velocities."""
+        npy of positions and velocities.  The frame's positions, velocities and
+        record are copied to the host here (a short copy of 24 bytes per
+        particle); with ``wait=False`` the files are then written by a
+        background thread while the caller goes on stepping (``flush`` waits
+        for them)."""
         d = self.config.dim[None]
         n = self.fluid.part_num[None]
         frame = self.globalvar.time_counter
-        for sub in ("ply", "json", "part_data"):
-            os.makedirs(os.path.join(self.out_dir, sub), exist_ok=True)
-        pos = self.fluid.pos[:n].cpu().numpy()
-        vel = self.fluid.vel[:n].cpu().numpy()
-        write_ply(os.path.join(self.out_dir, "ply", "fluid_pos"), frame, d, n, pos)
-        with open(os.path.join(self.out_dir, "json", "frame%d.json" % frame), "w") as f:
-            f.write(json.dumps(self.frame_record()))
-        np.save(os.path.join(self.out_dir, "part_data", "vel_%d" % frame), vel)
-        np.save(os.path.join(self.out_dir, "part_data", "pos_%d" % frame), pos)
+        out = self.out_dir
+        pos = self.fluid.pos[:n].detach().to("cpu", copy=True).numpy()
+        vel = self.fluid.vel[:n].detach().to("cpu", copy=True).numpy()
+        rec = json.dumps(self.frame_record())
+
+        def job():
+            for sub in ("ply", "json", "part_data"):
+                os.makedirs(os.path.join(out, sub), exist_ok=True)
+            write_ply(os.path.join(out, "ply", "fluid_pos"), frame, d, n, pos)
+            with open(os.path.join(out, "json", "frame%d.json" % frame), "w") as f:
+                f.write(rec)
+            np.save(os.path.join(out, "part_data", "vel_%d" % frame), vel)
+            np.save(os.path.join(out, "part_data", "pos_%d" % frame), pos)
+
+        if wait:
+            job()
+            return
+        if self._writer is None:
+            self._writer = FrameWriter()
+        self._writer.submit(job)
+
+    def flush(self):
+        """Waits until every frame passed to ``write_files(wait=False)`` is on disk."""
+        if self._writer is not None:
+            self._writer.flush()
