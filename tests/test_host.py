@@ -143,3 +143,33 @@ def test_map_grid_shape_matches_reference_run():
         assert abs(g.dist - ref["dist"]) <= 1e-7 * ref["dist"]
         import numpy as np
         np.testing.assert_allclose(g.pos[(0,) * len(g.shape)].numpy(), ref["lb"], rtol=0, atol=1e-7)
+
+
+def test_gather_scenes_concatenates_and_rebinds_views():
+    """gather_scenes (batched form, host side): every field of every scene lands
+    at its scene's offset of the concatenated sets, in scene order, and each
+    scene's per-set arrays become views of them (the reference-shaped
+    per-scene API reads and writes the batch)."""
+    import torch
+    from tichi_sph_gb300 import sph_config, workloads
+    from tichi_sph_gb300.batch import FIELDS, gather_scenes
+    from tichi_sph_gb300.simulation import Simulation
+    sims = []
+    for c, s in workloads.batched_dambreaks(n_scenes=3, n_min=200, n_max=800):
+        sim = Simulation(sph_config.Config(c, s), device="cpu")
+        sim.init_scenario()
+        sims.append(sim)
+    before = [{key: {f: getattr(getattr(s, key), f)[:getattr(s, key).part_num[None]].clone() for f in FIELDS}
+               for key in ("fluid", "bound")} for s in sims]
+    fluid, bound, nf, nb = gather_scenes(sims, device="cpu")
+    assert nf == [s.fluid.part_num[None] for s in sims] and nb == [s.bound.part_num[None] for s in sims]
+    assert fluid.part_num[None] == sum(nf) and bound.part_num[None] == sum(nb)
+    for big, key, counts in ((fluid, "fluid", nf), (bound, "bound", nb)):
+        off = 0
+        for i, (s, n) in enumerate(zip(sims, counts)):
+            for f in FIELDS:
+                assert torch.equal(getattr(big, f)[off:off + n], before[i][key][f]), (key, i, f)
+            # a write through the scene's view reaches the batch
+            getattr(s, key).pos[0, 0] = 123.0
+            assert float(getattr(big, "pos")[off, 0]) == 123.0
+            off += n
