@@ -173,3 +173,26 @@ def test_gather_scenes_concatenates_and_rebinds_views():
             getattr(s, key).pos[0, 0] = 123.0
             assert float(getattr(big, "pos")[off, 0]) == 123.0
             off += n
+
+
+def test_status_bits_become_warnings_once_per_condition():
+    """A step's status bits (TSPH_ST_*) reach the Python user as RuntimeWarnings,
+    each condition once per solver; the step itself goes on, as the reference
+    does."""
+    import warnings
+    from tichi_sph_gb300 import _native as N
+    both = N.ST_NONFINITE_POS | N.ST_OUTSIDE_GRID
+    assert len(N.status_messages(both)) == 2 and N.status_messages(0) == []
+    assert len(N.status_messages(N.ST_DIV_ITER_CAP | N.ST_DENS_ITER_CAP | N.ST_FBM_PASS_CAP)) == 3
+    w = N.StatusWarner(scene=2)
+    with warnings.catch_warnings(record=True) as got:
+        warnings.simplefilter("always")
+        w(0)
+        w(N.ST_OUTSIDE_GRID)
+        w(N.ST_OUTSIDE_GRID)            # already reported
+        w(both)                         # only the new condition
+        w(N.ST_DENS_ITER_CAP)
+    msgs = [str(x.message) for x in got]
+    assert all(x.category is RuntimeWarning for x in got)
+    assert len(msgs) == 3 and all(m.endswith("(scene 2)") for m in msgs)
+    assert "outside the neighbour grid" in msgs[0] and "not finite" in msgs[1] and "constant-density" in msgs[2]

@@ -6,6 +6,7 @@ missing, :func:`lib` raises, so nothing silently runs anywhere but the GPU.
 """
 import ctypes as C
 import os
+import warnings
 
 from . import build as _build
 
@@ -14,6 +15,40 @@ MAX_PHASES = 8
 OK, ERR_INVALID, ERR_CAPACITY, ERR_CUDA, ERR_STATE = 0, 1, 2, 3, 4
 ST_NONFINITE_POS, ST_DIV_ITER_CAP, ST_DENS_ITER_CAP, ST_FBM_PASS_CAP, ST_OUTSIDE_GRID = 1, 2, 4, 8, 16
 DFSPH, VFSPH = 0, 1
+
+_STATUS_TEXT = (
+    (ST_NONFINITE_POS, "a fluid or boundary position is not finite (the particle has no cell and no neighbours)"),
+    (ST_OUTSIDE_GRID, "particles lie outside the neighbour grid (sim_space_lb .. sim_space_rt) and have no "
+                      "neighbours"),
+    (ST_DIV_ITER_CAP, "the divergence-free solve stopped at solver_iter_threshold_max"),
+    (ST_DENS_ITER_CAP, "the constant-density solve stopped at solver_iter_threshold_max"),
+    (ST_FBM_PASS_CAP, "the volume-fraction pass loop stopped at its pass cap"),
+)
+
+
+def status_messages(status):
+    """The conditions a step's status bits (``TSPH_ST_*``) report, in words."""
+    return [text for bit, text in _STATUS_TEXT if status & bit]
+
+
+class StatusWarner:
+    """Reports a step's status bits as RuntimeWarnings, each condition once per
+    solver (and scene).  The reference goes on silently in all of these cases
+    (cells out of range are skipped, sph.py:52-60; the solver loops break at
+    their cap, main.py:213, 233), and so does the step; the warning only tells."""
+
+    def __init__(self, scene=None):
+        self.scene = scene
+        self.seen = 0
+
+    def __call__(self, status):
+        new = int(status) & ~self.seen
+        if not new:
+            return
+        self.seen |= new
+        where = "" if self.scene is None else " (scene %d)" % self.scene
+        for text in status_messages(new):
+            warnings.warn("tichi_sph_gb300: " + text + where, RuntimeWarning, stacklevel=3)
 
 _f = C.c_float
 _i32 = C.c_int32

@@ -91,6 +91,10 @@ class BatchSolver:
         with torch.cuda.device(self.device):
             check(self._lib.tsph_read_scene_stats(self.ctx, 0, self.n_scenes, self._stats, _stream(self.device)),
                   "tsph_read_scene_stats")
+        if getattr(self, "_warn", None) is None:
+            self._warn = [_native.StatusWarner(scene=i) for i in range(self.n_scenes)]
+        for w, s in zip(self._warn, self._stats):
+            w(s.status)
         return [{k: getattr(s, k) for k, _ in _native.Stats._fields_} for s in self._stats]
 
     def close(self):

@@ -45,6 +45,7 @@ class Solver:
         self.set_graph_mode(use_graph)
         self.tpp = 1
         self._stats = _native.Stats()
+        self._warn = _native.StatusWarner()
 
     def set_graph_mode(self, use_graph):
         check(self._lib.tsph_set_graph_mode(self.ctx, 1 if use_graph else 0), "tsph_set_graph_mode")
@@ -115,6 +116,7 @@ class Solver:
             check(self._lib.tsph_read_stats(self.ctx, _native.C.byref(self._stats),
                                             _native.C.c_void_p(_stream_handle(self.device))), "tsph_read_stats")
         s = self._stats
+        self._warn(s.status)
         self.config.dt[None] = s.dt
         self.fluid.compression[None] = s.compression
         self.fluid.statistics_kinetic_energy[None] = s.kinetic_energy
