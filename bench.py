@@ -8,7 +8,8 @@ Workload: the 3D single-phase DFSPH dam break (``workloads.dambreak_3d``): a
 566,742 boundary particles, h = 0.02, dt <= 2e-4 (CFL), density tolerance 0.1%,
 divergence tolerance 1%.  A step is one substep of the reference's ``run_step``
 (``cfl_condition`` + ``sph_step``, main.py:347-352) over the whole scene; the
-metric counts fluid particles only (SURVEY-defined particle-steps/s).
+metric counts fluid particles only (particle-steps/s = fluid particles x
+substeps / time; boundary particles are not counted).
 
 Output: one JSON line on rank 0.  ``value`` is timed with CUDA events on the
 solver's stream around K substeps whose inputs are already on the GPU; ``e2e``
@@ -16,7 +17,8 @@ times the same substeps through the public Python API with the fluid state
 copied from pinned host memory before each substep and positions / velocities
 and the step scalars copied back after it.  ``roofline`` takes the step phase
 with the largest share of the step time, its algorithmic bytes per launch
-(per-particle figures in the design doc) and its mean launch time measured here with
+(each particle's own fields once per sweep: ``ALGO_BYTES_3D``) and its mean
+launch time measured here with
 CUDA events (``tsph_profile_phases``).  ``cpu_baseline`` times the C
 restatement of the reference (``oracle/sph_port.c``, FP32, OpenMP on every host
 core) on a bounded number of substeps of the same scene.
