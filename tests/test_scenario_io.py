@@ -159,3 +159,17 @@ def test_background_write_error_surfaces_at_flush(tmp_path):
     with pytest.raises(OSError):
         sim.flush()
     sim.flush()  # the error is reported once
+
+
+def test_inlet_interval_branches(tmp_path):
+    """main.py:26-39 for an inlet whose normal has no downward gravity component
+    (dt = r rf / v, or no pushes at all at speed 0) and for a negative speed
+    (the normal and the speed both flip)."""
+    sim = _sim(tmp_path, [_cube([0.0, 0.0, 0.0], [0.1, 0.1, 0.1])])
+    r = float(np.float32(PS))
+    assert sim.inlet_helper_get_dt([0, 1, 0], 2.0, 1.5) == pytest.approx(r * 1.5 / 2.0)
+    assert sim.inlet_helper_get_dt([1, 0, 0], 0.5, 1.0) == pytest.approx(r / 0.5)
+    assert sim.inlet_helper_get_dt([0, 2, 0], 0.0, 1.0) == float("inf")
+    # speed -1 along +y is speed 1 along -y: gravity along the normal, the quadratic branch
+    a = 9.81
+    assert sim.inlet_helper_get_dt([0, 1, 0], -1.0, 1.0) == pytest.approx((np.sqrt(1 + 2 * a * r) - 1) / a)
