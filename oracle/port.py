@@ -1,8 +1,10 @@
 """ctypes driver of ``oracle/sph_port.c`` -- TEST INFRASTRUCTURE ONLY.
 
-The reference-structured C restatement (FP32, OpenMP) used as the timed CPU
-baseline and as a mid-size cross-check.  Particle arrays are host numpy arrays
-laid out exactly like the CUDA path's ``tsph_set`` views.
+The reference-structured C restatement (OpenMP) in two builds: FP32 (the
+reference's arithmetic; the timed CPU baseline and a mid-size cross-check) and
+FP64 (``fp64=True``: every sum and pair term in double over the FP32 particle
+arrays; the one-step oracle at the benchmark sizes).  Particle arrays are host
+numpy arrays laid out exactly like the CUDA path's ``tsph_set`` views.
 """
 import ctypes as C
 import os
@@ -20,14 +22,14 @@ class PortStats(C.Structure):
                 ("div_iter", C.c_int32), ("incom_iter", C.c_int32), ("fbm_passes", C.c_int32)]
 
 
-_LIB = None
+_LIBS = {}
 
 
-def lib():
-    global _LIB
-    if _LIB is None:
+def lib(fp64=False):
+    real = "double" if fp64 else "float"
+    if real not in _LIBS:
         from oracle import build_oracle
-        path = build_oracle.build()
+        path = build_oracle.build(real=real)
         L = C.CDLL(path)
         L.port_create.restype = C.c_void_p
         L.port_create.argtypes = [C.POINTER(_native.Params), C.c_int64, C.c_int64]
@@ -36,8 +38,8 @@ def lib():
         L.port_substep.restype = C.c_int
         L.port_substep.argtypes = [C.c_void_p, C.POINTER(_native.Set), C.POINTER(_native.Set), C.POINTER(PortStats)]
         L.port_num_threads.restype = C.c_int
-        _LIB = L
-    return _LIB
+        _LIBS[real] = L
+    return _LIBS[real]
 
 
 class HostSet:
@@ -76,27 +78,28 @@ class HostSet:
 class PortSim:
     """The C restatement stepping one (fluid, boundary) pair."""
 
-    def __init__(self, config, fluid_arrays, bound_arrays, fbm=False, fbm_max_passes=1000):
+    def __init__(self, config, fluid_arrays, bound_arrays, fbm=False, fbm_max_passes=1000, fp64=False):
         d, P = config.dim[None], config.phase_num[None]
+        self.L = lib(fp64)
         self.fluid = HostSet(len(fluid_arrays["pos"]), d, P, fluid_arrays)
         self.bound = HostSet(len(bound_arrays["pos"]), d, P, bound_arrays)
         self.params = config.to_params(fbm_enabled=fbm, fbm_max_passes=fbm_max_passes)
-        self.h = lib().port_create(C.byref(self.params), self.fluid.n, self.bound.n)
+        self.h = self.L.port_create(C.byref(self.params), self.fluid.n, self.bound.n)
         self.stats = PortStats()
 
     def set_state(self, time_count=0.0, compression=0.0):
-        lib().port_set_state(self.h, time_count, compression)
+        self.L.port_set_state(self.h, time_count, compression)
 
     def substep(self):
-        lib().port_substep(self.h, C.byref(self.fluid.s), C.byref(self.bound.s), C.byref(self.stats))
+        self.L.port_substep(self.h, C.byref(self.fluid.s), C.byref(self.bound.s), C.byref(self.stats))
         return {k: getattr(self.stats, k) for k, _ in PortStats._fields_}
 
     def threads(self):
-        return lib().port_num_threads()
+        return self.L.port_num_threads()
 
     def close(self):
         if self.h:
-            lib().port_destroy(self.h)
+            self.L.port_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -180,7 +180,9 @@ static void cfl_condition(port_ctx *c, obj_t *o) {
             if (t < dt) dt = t;
         }
     }
-    c->dt = dt;
+    /* config.dt is an f32 field in the reference (sph_config.py:100): the FP64
+     * build rounds it there too */
+    c->dt = (REAL)(float)dt;
 }
 
 static void prepare_attr(port_ctx *c, obj_t *o, obj_t *no) {
