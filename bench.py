@@ -6,10 +6,22 @@
 Workload: the 3D single-phase DFSPH dam break (``workloads.dambreak_3d``): a
 1 m cube of 1,000,000 fluid particles at 0.01 m in a 3 x 1.5 x 1 m tank of
 566,742 boundary particles, h = 0.02, dt <= 2e-4 (CFL), density tolerance 0.1%,
-divergence tolerance 1%.  A step is one substep of the reference's ``run_step``
-(``cfl_condition`` + ``sph_step``, main.py:347-352) over the whole scene; the
-metric counts fluid particles only (particle-steps/s = fluid particles x
-substeps / time; boundary particles are not counted).
+divergence tolerance 1%, 500 substeps from rest.  A step is one substep of the
+reference's ``run_step`` (``cfl_condition`` + ``sph_step``, main.py:347-352) over
+the whole scene; the metric counts fluid particles only (particle-steps/s =
+fluid particles x substeps / time; boundary particles are not counted).  The
+timed window is the end of the 500-substep run: the flow first develops for
+500 - W - K untimed substeps (``--develop``), then W warm-up and K timed
+substeps follow, so the pressure solves iterate as they do once the column has
+loaded the floor, not at their floor of two iterations as right after rest.
+
+The same line carries the other workloads of the hot path, each timed with CUDA
+events at N = 1: ``batched`` (256 dam breaks of uneven size in one launch
+against the same scenes stepped one at a time), ``twophase3d`` (2M-particle
+two-phase VFSPH with surface tension and the volume-fraction update, the end of
+its 300-substep run), ``dambreak2d`` (5,000-particle 2D dam break, substeps 4 to
+1,000 of its run) and ``adjoint`` (backward / forward time of the differentiable
+64-substep rollout of a 99,452-particle block).
 
 Output: one JSON line on rank 0.  ``value`` is timed with CUDA events on the
 solver's stream around K substeps whose inputs are already on the GPU; ``e2e``
@@ -316,8 +328,9 @@ def batched_line(res, args, ws):
                        "mean_div_iter": res["mean_div_iter"], "mean_incom_iter": res["mean_incom_iter"]}}
 
 
-def run_other(kind, steps, warmup, dev):
-    """The two-phase VFSPH block pair or the 2D dam break through the plain path."""
+def run_other(kind, steps, warmup, dev, develop=0):
+    """The two-phase VFSPH block pair or the 2D dam break through the plain path:
+    ``develop`` untimed substeps from rest, ``warmup`` more, then ``steps`` timed."""
     import numpy as np
     import torch
     from tichi_sph_gb300 import sph_config, workloads
@@ -338,7 +351,7 @@ def run_other(kind, steps, warmup, dev):
         sim.fluid.update_mass_all()
     s = sim.solver
     stream = torch.cuda.current_stream(dev)
-    for _ in range(warmup):
+    for _ in range(develop + warmup):
         s.substep()
     torch.cuda.synchronize(dev)
     s0 = s.stats()
@@ -353,7 +366,7 @@ def run_other(kind, steps, warmup, dev):
     vf = sim.fluid.volume_frac[:nf].cpu().numpy().astype(np.float64)
     s.close()
     return {"kind": kind, "fluid_particles": nf, "boundary_particles": sim.bound.part_num[None], "ms": ms,
-            "steps": steps, "warmup": warmup,
+            "steps": steps, "warmup": warmup, "develop": develop,
             "div": (s1["total_div_iter"] - s0["total_div_iter"]) / steps,
             "inc": (s1["total_incom_iter"] - s0["total_incom_iter"]) / steps,
             "fbm": (s1["total_fbm_passes"] - s0["total_fbm_passes"]) / steps,
@@ -374,6 +387,33 @@ def other_line(res, args, ws):
                        "mean_incom_iter": res["inc"], "mean_fbm_passes": res["fbm"],
                        "max_density_error": res["max_comp"], "max_abs_volume_fraction_sum_error": res["vf_sum_err"],
                        "min_volume_fraction": res["vf_min"]}}
+
+
+def extra_workloads(dev, args):
+    """The other configurations of the hot path at N = 1, for the headline line:
+    the two-phase VFSPH pair (end of its 300-substep run), the 2D dam break
+    (substeps 4..1,000 of its run) and the adjoint's backward / forward ratio."""
+    out = {}
+    tp = run_other("twophase3d", 20, 3, dev, develop=277)
+    out["twophase3d"] = {"value": tp["fluid_particles"] / (tp["ms"] / 1e3), "unit": UNIT, "ms_per_step": tp["ms"],
+                         "window": "substeps %d..%d of a 300-substep run from rest" % (
+                             tp["develop"] + tp["warmup"] + 1, tp["develop"] + tp["warmup"] + tp["steps"]),
+                         "workload": other_line(tp, args, 1)["config"]["workload"],
+                         **{k: other_line(tp, args, 1)["config"][k] for k in (
+                             "fluid_particles", "boundary_particles", "mean_div_iter", "mean_incom_iter",
+                             "mean_fbm_passes", "max_density_error", "max_abs_volume_fraction_sum_error")}}
+    d2 = run_other("dambreak2d", 997, 3, dev)
+    out["dambreak2d"] = {"value": d2["fluid_particles"] / (d2["ms"] / 1e3), "unit": UNIT, "ms_per_step": d2["ms"],
+                         "window": "substeps 4..1000 of the 1,000-substep run from rest",
+                         "workload": other_line(d2, args, 1)["config"]["workload"],
+                         **{k: other_line(d2, args, 1)["config"][k] for k in (
+                             "fluid_particles", "boundary_particles", "mean_div_iter", "mean_incom_iter",
+                             "max_density_error")}}
+    ad = run_adjoint(3, 1, dev)
+    al = adjoint_line(ad, args, 1)
+    out["adjoint"] = {"metric": "backward/forward time", "value": ad["ratio"], "unit": "ratio",
+                      "higher_is_better": False, "reps": ad["reps"], **al["config"]}
+    return out
 
 
 def run_adjoint(reps, warmup, dev, substeps=64, checkpoint_every=8, gamma=0.0):
@@ -449,8 +489,10 @@ def run_reference(args, rank, ws):
         "metric": METRIC, "value": res["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": len(res["iters"]), "warmup": 0, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "3D DFSPH dam break, %d fluid + %d boundary particles, h=%g, "
-                               "dt<=%g, rho tol 0.1%%" % (nf, res["n_bound"], 2 * args.spacing, args.spacing / 50),
+        "config": {"workload": "3D DFSPH dam break, %d fluid + %d boundary particles, h=%g, dt<=%g (CFL), "
+                               "rho tol 0.1%%, div tol 1%%" % (nf, res["n_bound"], 2 * args.spacing, args.spacing / 50),
+                   "window": "substeps 1..%d of the run from rest (a bounded CPU sample; the GPU arm times the "
+                             "end of the 500-substep run, where the solves iterate more)" % len(res["iters"]),
                    "fluid_particles": nf},
         "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -464,8 +506,13 @@ def run_reference(args, rank, ws):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--develop", type=int, default=-1,
+                    help="untimed substeps before the warm-up (-1: 500 - warmup - steps, so the timed window "
+                         "ends the 500-substep run)")
+    ap.add_argument("--run-length", type=int, default=500, help="substeps of the headline run (for --develop -1)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the two-phase, 2D and adjoint workloads")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-side", type=int, default=100)
     ap.add_argument("--gamma", type=float, default=0.0,
@@ -531,6 +578,9 @@ def main():
     tune = None
     if args.tpp:
         solver.set_threads_per_particle(args.tpp)
+    develop = args.develop if args.develop >= 0 else max(0, args.run_length - args.warmup - args.steps)
+    for _ in range(develop):
+        solver.substep()
     for i in range(args.warmup):
         solver.substep()
         if i == 0 and not args.tpp:
@@ -647,6 +697,11 @@ def main():
         batched["workload"] = ("%d independent 3D dam breaks, fluid counts log-uniform in [2k, 200k] (seed 4), "
                                "batched in one launch vs stepped one at a time through the plain path" % b["n_scenes"])
 
+    extra = {}
+    if ws == 1 and not args.no_extra:
+        solver.close()
+        extra = extra_workloads(dev, args)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(args.n_side, budget_s=args.cpu_budget, max_steps=20, spacing=args.spacing)
@@ -658,10 +713,12 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "3D DFSPH dam break, %d fluid + %d boundary particles, h=%g, dt<=%g (CFL), "
-                                   "rho tol 0.1%%, div tol 1%%, from rest" % (nf, nb, 2 * args.spacing,
-                                                                             args.spacing / 50),
+                                   "rho tol 0.1%%, div tol 1%%" % (nf, nb, 2 * args.spacing, args.spacing / 50),
+                       "window": "substeps %d..%d of the run from rest (%d untimed to develop the flow, %d warm-up)" % (
+                           develop + args.warmup + 1, develop + args.warmup + args.steps, develop, args.warmup),
                        "fluid_particles": nf, "boundary_particles": nb, "parallelism": "replicas" if ws > 1 else "single",
                        "mean_div_iter": k_div, "mean_incom_iter": k_inc,
+                       "density_error_after_window": s1["compression"],
                        "max_density_error": s1["max_dens_compression"],
                        "l2": "inputs larger than L2 (per-step state ~%d MB > 129 MB)" % round(400 * nf / 1e6),
                        "threads_per_particle": solver.tpp, "autotune_ms": tune,
@@ -675,8 +732,10 @@ def main():
             "clocks": clk,
             "batched": batched,
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
-    solver.close()
+    if solver.ctx:
+        solver.close()
     if dist:
         dist.destroy_process_group()
     return 0
