@@ -173,3 +173,30 @@ def test_inlet_interval_branches(tmp_path):
     # speed -1 along +y is speed 1 along -y: gravity along the normal, the quadratic branch
     a = 9.81
     assert sim.inlet_helper_get_dt([0, 1, 0], -1.0, 1.0) == pytest.approx((np.sqrt(1 + 2 * a * r) - 1) / a)
+
+
+def test_frame_writer_queue_is_bounded():
+    """A writer slower than the solver holds submit back once max_pending frames
+    wait, instead of letting their host copies pile up."""
+    import threading
+    from tichi_sph_gb300.simulation import FrameWriter
+    w = FrameWriter(max_pending=2)
+    gate = threading.Event()
+    started = threading.Event()
+
+    def slow():
+        started.set()
+        gate.wait(10)
+
+    w.submit(slow)
+    started.wait(10)
+    w.submit(lambda: None)
+    w.submit(lambda: None)  # the queue now holds its two frames
+    t = threading.Thread(target=lambda: w.submit(lambda: None))
+    t.start()
+    t.join(0.2)
+    assert t.is_alive()  # the fourth frame waits for room
+    gate.set()
+    t.join(10)
+    assert not t.is_alive()
+    w.flush()

@@ -27,11 +27,13 @@ def main(argv=None):
     sim.init_scenario()
     print("fluid particle count: ", sim.fluid.part_num[None])
     print("bound particle count: ", sim.bound.part_num[None])
-    while sim.globalvar.time_count < a.until:
-        sim.run_step(verbose=True)
-        if a.write:
-            sim.write_files(wait=False)  # files written in the background while stepping on
-    sim.flush()
+    try:
+        while sim.globalvar.time_count < a.until:
+            sim.run_step(verbose=True)
+            if a.write:
+                sim.write_files(wait=False)  # files written in the background while stepping on
+    finally:
+        sim.flush()  # the frames submitted so far reach the disk even if a step raised
     return 0
 
 

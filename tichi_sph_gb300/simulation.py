@@ -69,11 +69,13 @@ def write_ply(path, frame_num, dim, num, pos):
 class FrameWriter:
     """Writes frames' files in submission order on one background thread, so
     that the time loop goes on while a frame's PLY / JSON / npy files are
-    written.  ``flush`` waits for every submitted frame and re-raises the first
-    error a write met."""
+    written.  At most ``max_pending`` frames wait at a time: ``submit`` blocks
+    while that many are queued, so a disk slower than the solver holds the time
+    loop back instead of piling up host copies.  ``flush`` waits for every
+    submitted frame and re-raises the first error a write met."""
 
-    def __init__(self):
-        self._q = queue.Queue()
+    def __init__(self, max_pending=4):
+        self._q = queue.Queue(maxsize=max_pending)
         self._thread = None
         self._err = None
 
@@ -101,6 +103,65 @@ class FrameWriter:
             raise err
 
 
+class _FrameSlot:
+    """One frame in flight from a CUDA device: a device snapshot of positions and
+    velocities (taken on the solver's stream, so the next substep may overwrite
+    the particle arrays at once), pinned host buffers, and the side stream's
+    copy event that the writer waits on."""
+
+    def __init__(self, n, dim, device):
+        import torch
+        self.dev = torch.empty((2, n, dim), dtype=torch.float32, device=device)
+        self.host = torch.empty((2, n, dim), dtype=torch.float32, pin_memory=True)
+        self.done = None
+
+
+class _AsyncFrames:
+    """Device-to-host copies of frames that do not synchronise the solver's
+    stream: a device-to-device snapshot on the solver's stream (microseconds),
+    then the device-to-host copy on a side stream, which the writer thread waits
+    for by its event.  Up to ``slots`` frames are in flight; a new frame reuses a
+    slot once that slot's files are written."""
+
+    def __init__(self, device, slots=3):
+        import torch
+        self.device = device
+        self.stream = torch.cuda.Stream(device=device)
+        self.free = queue.Queue()
+        self.slots = slots
+        self.made = 0
+
+    def _take(self, n, dim):
+        try:
+            slot = self.free.get_nowait()
+        except queue.Empty:
+            if self.made < self.slots:
+                self.made += 1
+                return _FrameSlot(n, dim, self.device)
+            slot = self.free.get()
+        if slot.dev.shape[1] < n or slot.dev.shape[2] != dim:
+            slot = _FrameSlot(n, dim, self.device)  # the particle count outgrew it
+        return slot
+
+    def snapshot(self, pos, vel):
+        """Enqueues the copies; returns (slot, host views of pos and vel)."""
+        import torch
+        n, dim = pos.shape
+        slot = self._take(n, dim)
+        main = torch.cuda.current_stream(self.device)
+        slot.dev[0, :n].copy_(pos)
+        slot.dev[1, :n].copy_(vel)
+        self.stream.wait_stream(main)
+        with torch.cuda.stream(self.stream):
+            slot.host[:, :n].copy_(slot.dev[:, :n], non_blocking=True)
+            slot.done = torch.cuda.Event()
+            slot.done.record(self.stream)
+        return slot, slot.host[0, :n], slot.host[1, :n]
+
+    def release(self, slot):
+        self.free.put(slot)
+
+
 class Simulation:
     """The reference's module-level state of ``main.py`` as one object."""
 
@@ -120,6 +181,7 @@ class Simulation:
         self.out_dir = out_dir or config.solver_type
         self._solver = None
         self._writer = None
+        self._frames = None
 
     @property
     def solver(self):
@@ -271,20 +333,20 @@ class Simulation:
 
     def write_files(self, wait=True):
         """``main.py:371-378`` without the PNG: PLY of fluid positions, frame JSON,
-        npy of positions and velocities.  The frame's positions, velocities and
-        record are copied to the host here (a short copy of 24 bytes per
-        particle); with ``wait=False`` the files are then written by a
-        background thread while the caller goes on stepping (``flush`` waits
-        for them)."""
+        npy of positions and velocities.  With ``wait=True`` the frame is copied
+        to the host and written before returning.  With ``wait=False`` nothing
+        waits for the GPU: on a CUDA device the positions and velocities are
+        snapshotted on the solver's stream and copied to pinned host memory on a
+        side stream, and a background thread writes the files once that copy has
+        finished, while the caller goes on stepping (``flush`` waits for every
+        frame)."""
         d = self.config.dim[None]
         n = self.fluid.part_num[None]
         frame = self.globalvar.time_counter
         out = self.out_dir
-        pos = self.fluid.pos[:n].detach().to("cpu", copy=True).numpy()
-        vel = self.fluid.vel[:n].detach().to("cpu", copy=True).numpy()
         rec = json.dumps(self.frame_record())
 
-        def job():
+        def write(pos, vel):
             for sub in ("ply", "json", "part_data"):
                 os.makedirs(os.path.join(out, sub), exist_ok=True)
             write_ply(os.path.join(out, "ply", "fluid_pos"), frame, d, n, pos)
@@ -293,11 +355,28 @@ class Simulation:
             np.save(os.path.join(out, "part_data", "vel_%d" % frame), vel)
             np.save(os.path.join(out, "part_data", "pos_%d" % frame), pos)
 
+        fpos, fvel = self.fluid.pos[:n].detach(), self.fluid.vel[:n].detach()
         if wait:
-            job()
+            write(fpos.to("cpu", copy=True).numpy(), fvel.to("cpu", copy=True).numpy())
             return
         if self._writer is None:
             self._writer = FrameWriter()
+        if fpos.device.type != "cuda":
+            pos, vel = fpos.clone().numpy(), fvel.clone().numpy()
+            self._writer.submit(lambda: write(pos, vel))
+            return
+        if self._frames is None:
+            self._frames = _AsyncFrames(fpos.device)
+        frames = self._frames
+        slot, hpos, hvel = frames.snapshot(fpos, fvel)
+
+        def job():
+            try:
+                slot.done.synchronize()
+                write(hpos.numpy(), hvel.numpy())
+            finally:
+                frames.release(slot)
+
         self._writer.submit(job)
 
     def flush(self):
