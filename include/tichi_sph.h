@@ -217,15 +217,17 @@ int tsph_profile_phases(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bo
 
 /* Fluid density sweep that allocates nothing.  No counterpart in the reference:
  * it exists for callers that cannot allocate device memory where they call in
- * (inside a stream capture, under a host that pre-plans all device memory, or
- * beside an allocator that owns the device) and so cannot hold a tsph_ctx.
+ * (under a host that pre-plans all device memory, or beside an allocator that
+ * owns the device) and so cannot hold a tsph_ctx.
  * From caller-owned device arrays (positions [n][dim], masses, rest volumes of
  * the fluid and boundary sets) it writes W, sph_density and sph_compression of
  * every fluid particle -- the sums sph_step's density sweep forms from the same
  * positions.  Working memory is one fixed device array shared by all calls:
  * node_num <= TSPH_NOALLOC_MAX_CELLS and n <= TSPH_NOALLOC_MAX_PARTICLES per set,
  * larger inputs return TSPH_ERR_CAPACITY; calls that overlap on the GPU race.
- * The first call on a device looks the array up (make it before any capture).
+ * The first call on a device looks the array up in the device's primary
+ * context and caches the address (make it before any stream capture; a later
+ * cudaDeviceReset or a non-primary context is not supported).
  * Stream-ordered; does not synchronise. */
 int tsph_fluid_density_noalloc(const tsph_params *params, const float *fluid_pos, const float *fluid_mass,
                                const float *fluid_rest_volume, int64_t n_fluid, const float *bound_pos,

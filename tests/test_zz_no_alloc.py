@@ -1,8 +1,8 @@
 """The density sweep that allocates nothing, against the solver step (needs a GPU).
 
 ``tsph_fluid_density_noalloc`` serves callers that cannot allocate device memory
-where they call in (inside a stream capture, or under a host that owns all
-device memory) and therefore cannot create a solver context.  Its W /
+where they call in (a host that pre-plans all device memory, or an allocator
+that owns the device) and therefore cannot create a solver context.  Its W /
 sph_density / sph_compression must equal those the regular step
 (``tsph_substep``) computes from the same positions, within the one-step
 tolerance of the parity tests (1e-5 of each field's scale) -- on two calls in a
@@ -66,7 +66,7 @@ def _close(a, b, name):
     assert err <= TOL, "%s: rel err %.3g" % (name, err)
 
 
-@pytest.mark.parametrize("scene", ["dfsph3d", "vfsph2d"])
+@pytest.mark.parametrize("scene", ["dfsph3d", "vfsph2d", "edge2d"])
 def test_noalloc_density_matches_step_two_calls(scene):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")

@@ -1,11 +1,10 @@
 // Fluid density sweep that allocates nothing: tsph_fluid_density_noalloc.
 //
 // Who needs it: callers that must not allocate device memory at the point they
-// call in -- code running while a CUDA stream is being captured into a graph
-// (cudaMalloc is not a capturable operation and fails the capture), plugin and
-// real-time hosts that pre-plan every byte of device memory and forbid
-// allocations on their worker threads, and embedders whose own allocator owns
-// the device.  They cannot hold a tsph_ctx (tsph_create allocates), so this
+// call in -- plugin and real-time hosts that pre-plan every byte of device
+// memory and forbid allocations on their worker threads, and embedders whose
+// own allocator owns the device (a cudaMalloc behind its back breaks its
+// accounting or fails for want of memory it has already reserved).  They cannot hold a tsph_ctx (tsph_create allocates), so this
 // entry point computes the fluid's SPH_prepare_attr sums (W, sph_density,
 // sph_compression over fluid and boundary neighbours; sph.py:50-64, called as
 // main.py:188-189) from caller-owned inputs into caller-owned outputs.
@@ -22,7 +21,10 @@
 // symbol is a host-side stand-in).  The first call on each device therefore
 // looks the address up with cudaGetSymbolAddress while that device is current,
 // checks the result and caches it; make that first call before any stream
-// capture begins, since the lookup is not a capturable operation.
+// capture begins, since the lookup is not a capturable operation.  The cached
+// address belongs to the device's primary context as it was at that first
+// call: a cudaDeviceReset afterwards, or calls from a context other than the
+// primary one, are not supported.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -260,6 +262,9 @@ extern "C" int tsph_fluid_density_noalloc(const tsph_params *p, const float *flu
         return na_fail(TSPH_ERR_INVALID, "tsph_fluid_density_noalloc: null array");
     if (n_fluid == 0) return TSPH_OK;
 
+    // an error left pending by an earlier call of the caller is not this call's:
+    // take it off so that the check after the launches reports only these
+    (void)cudaGetLastError();
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return na_fail_cuda(e, "cudaGetDevice");
@@ -289,9 +294,10 @@ extern "C" int tsph_fluid_density_noalloc(const tsph_params *p, const float *flu
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t nn = p->node_num;
     // the scratch keeps the previous call's contents: clear the counters
-    cudaMemsetAsync(g.count[0], 0, sizeof(int) * nn, st);
-    cudaMemsetAsync(g.count[1], 0, sizeof(int) * nn, st);
-    cudaMemsetAsync(g.tail, 0, sizeof(int) * 2, st);
+    e = cudaMemsetAsync(g.count[0], 0, sizeof(int) * nn, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(g.count[1], 0, sizeof(int) * nn, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(g.tail, 0, sizeof(int) * 2, st);
+    if (e != cudaSuccess) return na_fail_cuda(e, "tsph_fluid_density_noalloc: clearing the scratch counters");
     const SetIn fi = {fluid_pos, fluid_mass, fluid_rest_volume, n_fluid};
     const SetIn bi = {bound_pos, bound_mass, bound_rest_volume, n_bound};
     const int bs = 256;
