@@ -1,8 +1,9 @@
 """Generate golden vectors by running the Tichi_SPH reference's own kernels.
 
-Test infrastructure, run by hand in a container that holds the reference source
-(``python tests/golden/make_golden.py [scene ...]``); the fixtures it writes are
-committed and the tests never need the reference at run time.
+Test infrastructure, run by hand where the reference source is present
+(``TICHI_REFERENCE=<Tichi_SPH tree> python tests/golden/make_golden.py [scene ...]``);
+the fixtures it writes are committed and the tests never need the reference at
+run time.
 
 Taichi is not installed here, so the reference modules are imported on top of the
 pure-Python Taichi stand-in in ``tests/golden/taichi_shim`` and every kernel body of
@@ -38,7 +39,7 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("TICHI_REFERENCE", "/root/reference")
+REF = os.environ.get("TICHI_REFERENCE", "")
 SCENES = os.path.join(HERE, "scenes")
 STEPS = {"dfsph2d": 3, "dfsph2d_r2": 2, "dfsph3d": 2, "vfsph2d": 3, "vfsph3d": 2, "edge2d": 2,
          "wcsph2d": 3, "wcsph3d": 2}
@@ -56,6 +57,8 @@ STATE_IN = ["pos", "vel", "volume_frac", "rest_volume", "mass", "rest_density"]
 
 
 def _child(scene, mode):
+    if not REF or not os.path.isdir(REF):
+        raise SystemExit("set TICHI_REFERENCE to the Tichi_SPH source tree (the folder holding sph.py)")
     sys.dont_write_bytecode = True
     sys.path.insert(0, os.path.join(HERE, "taichi_shim"))
     sys.path.insert(0, REF)
