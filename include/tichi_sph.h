@@ -172,6 +172,79 @@ int tsph_sph_step(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, v
 /* One substep of run_step (main.py:348-352): cfl_condition, clock, sph_step. */
 int tsph_substep(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, void *stream);
 
+/* ------------------------------------------------- kernel-level composition
+ * sph_step (main.py:175-256) split at the reference's own seams, for callers
+ * that compose the step themselves as main.py does from the kernels of
+ * sph.py.  One-scene contexts only.  The same kernels as tsph_sph_step run in
+ * the same order, so a step composed of these calls in main.py's order equals
+ * tsph_sph_step bit for bit.  Between tsph_grid_build and tsph_update the
+ * step's state lives in the context in cell order: the caller's arrays are read
+ * by tsph_grid_build and written by tsph_update only.  Calls out of order
+ * return TSPH_ERR_STATE. */
+enum { TSPH_SOLVE_DIV = 0, TSPH_SOLVE_DENS = 1 };
+enum {
+    TSPH_TERM_GRAVITY = 1,          /* SPH_advection_gravity_acc, sph.py:108-111 */
+    TSPH_TERM_VISCOSITY = 2,        /* SPH_advection_viscosity_acc, sph.py:114-129 */
+    TSPH_TERM_SURFACE_TENSION = 4,  /* SPH_advection_surface_tension_acc, sph.py:132-166 */
+    TSPH_TERM_ALL = 7
+};
+
+/* Starts a step: Ngrid.clear_node / encode / mem_shift / fill_node
+ * (sph_obj.py:295-323, main.py:178-183), SPH_clean_value (sph.py:22-38,
+ * main.py:185-186) and the gather of both sets into cell order with
+ * v_adv = vel (SPH_vel_2_vel_adv, sph.py:253-256, main.py:200). */
+int tsph_grid_build(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, void *stream);
+
+/* SPH_prepare_attr (f,f)(f,b)(b,b)(b,f), SPH_prepare_alpha_1 (f,f)(f,b),
+ * SPH_prepare_alpha_2 (f,f)(b,f), SPH_prepare_alpha (f)(b): sph.py:50-105 as
+ * main.py:188-197 calls them. */
+int tsph_density_alpha(tsph_ctx *ctx, void *stream);
+
+/* One Jacobi sweep A of a pressure solve: IPPE_adv_psi_init, IPPE_adv_psi
+ * (f,f)(f,b) and IPPE_psi_adv_non_negative (sph.py:196-226; main.py:203-208 or
+ * 224-229).  kind: TSPH_SOLVE_DIV before tsph_nonpressure, TSPH_SOLVE_DENS after.
+ * If compression_out is not NULL, synchronises and writes fluid.compression,
+ * the mean of psi_adv / psi0 over the fluid that the loop test reads. */
+int tsph_adv_psi(tsph_ctx *ctx, int kind, double *compression_out, void *stream);
+
+/* Sweep B: IPPE_update_vel_adv (f,f)(f,b), sph.py:229-244 (main.py:209-210 or
+ * 230-231); counts one iteration of the solve `kind`. */
+int tsph_update_vel_adv(tsph_ctx *ctx, int kind, void *stream);
+
+/* A whole solver loop, main.py:199-214 (kind TSPH_SOLVE_DIV) or 221-234
+ * (TSPH_SOLVE_DENS): while it < it_min or compression > tol, one sweep A and
+ * one sweep B; stops after it_max + 1 iterations.  tol < 0, it_min < 0 or
+ * it_max < 0 take the scene's own value (solver_divergence_threshold or
+ * solver_compression_threshold, solver_iter_threshold_min / _max).  Host
+ * driven, reading the compression after every sweep A as the reference does;
+ * writes the iterations run and the final compression. */
+int tsph_solve(tsph_ctx *ctx, int kind, double tol, int32_t it_min, int32_t it_max, int32_t *it_out,
+               double *err_out, void *stream);
+
+/* SPH_vel_adv_2_vel, the non-pressure forces selected by `terms`
+ * (TSPH_TERM_* bits; surface tension only where the scene's gamma is not 0) and
+ * SPH_advection_update_vel_adv: sph.py:108-166, 247-262 as main.py:215-220
+ * calls them.  Makes the predicted v_adv the density solve's start. */
+int tsph_nonpressure(tsph_ctx *ctx, int32_t terms, void *stream);
+
+/* The weakly compressible pressure block, main.py:238-242: WC_pressure_val,
+ * WC_pressure_acce (f,f)(f,b), SPH_advection_update_vel_adv (sph.py:169-193,
+ * 247-250).  Needs a context created with wcsph_enabled. */
+int tsph_wc_pressure(tsph_ctx *ctx, const tsph_set *bound, void *stream);
+
+/* One pass of the volume-fraction loop, main.py:244-248: SPH_FBM_clean_tmp,
+ * SPH_FBM_convect, SPH_FBM_diffuse, SPH_FBM_check_tmp (sph.py:301-372); the
+ * first pass of a step also computes the drift velocities.  Synchronises and
+ * writes fluid.general_flag (1 while some particle was flagged this pass).  A
+ * pass after the loop has ended (general_flag 0, or fbm_max_passes reached)
+ * does nothing.  Needs a context created with fbm_enabled. */
+int tsph_fbm_pass(tsph_ctx *ctx, int32_t *general_flag_out, void *stream);
+
+/* Ends the step: SPH_update_volume_frac (with fbm_enabled), SPH_update_mass,
+ * SPH_update_pos, SPH_update_energy (sph.py:265-286, 375-379; main.py:251-256)
+ * and the write-back of every field into the caller's arrays. */
+int tsph_update(tsph_ctx *ctx, const tsph_set *fluid, const tsph_set *bound, void *stream);
+
 /* Synchronises `stream` and copies the scalars of the last step (scene 0). */
 int tsph_read_stats(tsph_ctx *ctx, tsph_stats *out, void *stream);
 

@@ -196,3 +196,102 @@ def test_status_bits_become_warnings_once_per_condition():
     assert all(x.category is RuntimeWarning for x in got)
     assert len(msgs) == 3 and all(m.endswith("(scene 2)") for m in msgs)
     assert "outside the neighbour grid" in msgs[0] and "not finite" in msgs[1] and "constant-density" in msgs[2]
+
+
+class _FakeSet:
+    def __init__(self):
+        from tichi_sph_gb300.sph_obj import Scalar
+        self.compression = Scalar(0.0)
+        self.general_flag = Scalar(0)
+
+
+class _FakeSolver:
+    """Records the phase entries a composed step reaches (no GPU)."""
+
+    def __init__(self, fbm=False, compressions=()):
+        from tichi_sph_gb300.sph import _Composer
+        self.fluid, self.bound = _FakeSet(), _FakeSet()
+        self.fbm = fbm
+        self.log = []
+        self.comp = list(compressions)
+        self.flags = [1, 1, 0]
+        self.composer = _Composer(self)
+        self.fluid._solver = self.bound._solver = self
+
+    def grid_build(self):
+        self.log.append("grid")
+
+    def density_alpha(self):
+        self.log.append("density")
+
+    def adv_psi(self, kind):
+        self.log.append("psi%d" % kind)
+        return self.comp.pop(0) if self.comp else 0.0
+
+    def update_vel_adv(self, kind):
+        self.log.append("vel%d" % kind)
+
+    def nonpressure(self, terms):
+        self.log.append("nonpressure%d" % terms)
+
+    def wc_pressure(self):
+        self.log.append("wc")
+
+    def fbm_pass(self):
+        self.log.append("fbm")
+        return self.flags.pop(0)
+
+    def update(self):
+        self.log.append("update")
+
+    def stats(self):
+        self.log.append("stats")
+
+
+def test_composed_step_reaches_the_phase_entries():
+    """main.py:175-256 written with the reference-named kernels reaches the
+    phase entries in order, one call per group; the Python solver loops follow
+    the compression each sweep A reports, and the volume-fraction loop the
+    general flag of each pass."""
+    from tests.test_gpu_kernel_level import reference_shaped_sph_step
+    from tichi_sph_gb300 import Ngrid
+    from tichi_sph_gb300.sph_config import load
+    from tests import golden_io as G
+    cfg = load(*G.paths("vfsph2d"))
+    # divergence: 2 iterations (floor); density: a third one while above 1e-3 ... then below
+    fake = _FakeSolver(fbm=True, compressions=[0.0, 0.0, 0.5, 0.5, 1e-4])
+    ng = Ngrid(cfg)
+    ng._solver = fake
+    assert reference_shaped_sph_step(cfg, ng, fake.fluid, fake.bound, fbm=True, wc=True) == (2, 3)
+    assert fake.log == ["grid", "density", "psi0", "vel0", "psi0", "vel0", "nonpressure7", "psi1", "vel1", "psi1",
+                        "vel1", "psi1", "vel1", "wc", "fbm", "fbm", "fbm", "update", "stats"]
+    assert fake.fluid.compression[None] == 1e-4 and fake.fluid.general_flag[None] == 0
+    fake.log.clear()
+    fake.flags = [0]
+    reference_shaped_sph_step(cfg, ng, fake.fluid, fake.bound, fbm=True, viscosity=False)
+    assert "nonpressure5" in fake.log  # gravity + surface tension, no viscosity
+
+
+def test_composed_step_incomplete_group_raises():
+    from tichi_sph_gb300 import Ngrid, sph as S
+    from tichi_sph_gb300._native import TsphError
+    fake = _FakeSolver()
+    fl, bd = fake.fluid, fake.bound
+    ng = Ngrid(None)
+    ng._solver = fake
+    for f in (ng.clear_node, lambda: ng.encode(fl), lambda: ng.encode(bd), ng.mem_shift, lambda: ng.fill_node(fl),
+              lambda: ng.fill_node(bd), lambda: S.SPH_clean_value(fl)):
+        f()
+    assert fake.log == []  # the grid group waits for its last call
+    S.SPH_clean_value(bd)
+    assert fake.log == ["grid"] and fl.general_flag[None] == 1
+    S.SPH_prepare_attr(ng, fl, fl)
+    with pytest.raises(TsphError, match=r"SPH_prepare_attr\(fb\)"):
+        S.IPPE_adv_psi_init(fl)
+    with pytest.raises(TsphError, match="twice"):
+        S.SPH_prepare_attr(ng, fl, fl)
+        S.SPH_prepare_attr(ng, fl, fl)
+    with pytest.raises(TsphError, match="does not belong"):
+        S.SPH_prepare_attr(ng, fl, _FakeSet())
+    with pytest.raises(RuntimeError, match="no solver"):
+        Ngrid(None).clear_node()

@@ -15,6 +15,8 @@ MAX_PHASES = 8
 OK, ERR_INVALID, ERR_CAPACITY, ERR_CUDA, ERR_STATE = 0, 1, 2, 3, 4
 ST_NONFINITE_POS, ST_DIV_ITER_CAP, ST_DENS_ITER_CAP, ST_FBM_PASS_CAP, ST_OUTSIDE_GRID = 1, 2, 4, 8, 16
 DFSPH, VFSPH = 0, 1
+SOLVE_DIV, SOLVE_DENS = 0, 1
+TERM_GRAVITY, TERM_VISCOSITY, TERM_SURFACE_TENSION, TERM_ALL = 1, 2, 4, 7
 
 _STATUS_TEXT = (
     (ST_NONFINITE_POS, "a fluid or boundary position is not finite (the particle has no cell and no neighbours)"),
@@ -133,6 +135,16 @@ SIGNATURES = {
                                        C.POINTER(C.c_double), C.c_void_p]),
     "tsph_density_adjoint": (C.c_int, [CtxP, C.c_void_p, C.c_int, _fp, _fp, C.c_void_p]),
     "tsph_set_viscosity": (C.c_int, [CtxP, C.c_int, C.c_float]),
+    "tsph_grid_build": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p]),
+    "tsph_density_alpha": (C.c_int, [CtxP, C.c_void_p]),
+    "tsph_adv_psi": (C.c_int, [CtxP, C.c_int, C.POINTER(C.c_double), C.c_void_p]),
+    "tsph_update_vel_adv": (C.c_int, [CtxP, C.c_int, C.c_void_p]),
+    "tsph_solve": (C.c_int, [CtxP, C.c_int, C.c_double, _i32, _i32, C.POINTER(_i32), C.POINTER(C.c_double),
+                             C.c_void_p]),
+    "tsph_nonpressure": (C.c_int, [CtxP, _i32, C.c_void_p]),
+    "tsph_wc_pressure": (C.c_int, [CtxP, C.POINTER(Set), C.c_void_p]),
+    "tsph_fbm_pass": (C.c_int, [CtxP, C.POINTER(_i32), C.c_void_p]),
+    "tsph_update": (C.c_int, [CtxP, C.POINTER(Set), C.POINTER(Set), C.c_void_p]),
     "tsph_version": (C.c_char_p, []),
     "tsph_last_error": (C.c_char_p, []),
 }

@@ -219,8 +219,10 @@ int bind_sets(tsph_ctx *c, const tsph_set *f, const tsph_set *b) {
             return fail(TSPH_ERR_CAPACITY, "particle counts differ from the scene counts given at tsph_create_batch");
         return TSPH_OK;
     }
-    if (f->n > h.f_slots || b->n > h.b_slots)
+    if (f->n > c->cap_f || b->n > c->cap_b)
         return fail(TSPH_ERR_CAPACITY, "part_num above the capacity given at tsph_create");
+    if (f->n > f->capacity || b->n > b->capacity)
+        return fail(TSPH_ERR_CAPACITY, "part_num above the capacity of the set's own arrays");
     if (f->n != h.f_n || b->n != h.b_n) {
         h.f_n = f->n;
         h.b_n = b->n;
@@ -345,6 +347,8 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     c.p = ps[0];
     c.n_scenes = S;
     c.batch = batch;
+    c.cap_f = capf;
+    c.cap_b = capb;
     c.tpp = 1;
     c.use_graph = 1;
 
@@ -418,6 +422,7 @@ int create_impl(const tsph_params *ps, int S, const int64_t *fn, const int64_t *
     F.pos = A.get<float4>(fcap);
     F.mv = A.get<float2>(fcap);
     F.mpsi = A.get<float4>(fcap);
+    F.psilo = A.get<float>(fcap);
     F.rho0 = A.get<float>(fcap);
     F.vel = A.get<float4>(fcap);
     F.vadv = A.get<float4>(2 * fcap);
@@ -622,6 +627,194 @@ int tsph_sph_step(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *strea
 
 int tsph_substep(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream) {
     return run_step(c, f, b, stream, true);
+}
+
+// ----------------------------------------------------------- kernel-level composition
+// The phases of enqueue_step one call at a time; the caller runs the solver and
+// volume-fraction loops on the host, as main.py:199-250 does.
+
+static int kl_check(tsph_ctx *c, const char *what) {
+    if (!c) return fail(TSPH_ERR_INVALID, "null ctx");
+    if (c->n_scenes != 1) {
+        std::snprintf(g_last_error, sizeof(g_last_error), "%s: kernel-level calls take a one-scene context", what);
+        return TSPH_ERR_INVALID;
+    }
+    return TSPH_OK;
+}
+
+static int kl_state(const char *what, const char *need) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s called out of order: %s", what, need);
+    return TSPH_ERR_STATE;
+}
+
+// scene 0's per-step scalars, after the work enqueued on `st`
+static int kl_read_step(tsph_ctx *c, cudaStream_t st) {
+    TSPH_CK(cudaMemcpyAsync(c->host_ss, c->k.ss, sizeof(SceneStep), cudaMemcpyDeviceToHost, st));
+    TSPH_CK(cudaMemcpyAsync(c->host_sp, c->k.sp, sizeof(ScenePersist), cudaMemcpyDeviceToHost, st));
+    TSPH_CK(cudaStreamSynchronize(st));
+    return TSPH_OK;
+}
+
+int tsph_grid_build(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream) {
+    int rc = kl_check(c, "tsph_grid_build");
+    if (rc) return rc;
+    rc = bind_sets(c, f, b);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    launch_step_begin(*c, st);
+    launch_grid_build(*c, *f, *b, st, false);
+    TSPH_CK(cudaGetLastError());
+    c->kl_phase = 1;
+    c->kl_psi = 0;
+    c->kl_fbm = 0;
+    return TSPH_OK;
+}
+
+int tsph_density_alpha(tsph_ctx *c, void *stream) {
+    int rc = kl_check(c, "tsph_density_alpha");
+    if (rc) return rc;
+    if (c->kl_phase != 1) return kl_state("tsph_density_alpha", "it follows tsph_grid_build");
+    cudaStream_t st = (cudaStream_t)stream;
+    launch_density(*c, st);
+    launch_solve_begin(*c, kSolveDiv, 0, 0, st);
+    TSPH_CK(cudaGetLastError());
+    c->kl_phase = 2;
+    return TSPH_OK;
+}
+
+static int kl_solve_phase(tsph_ctx *c, int kind, const char *what) {
+    if (kind != TSPH_SOLVE_DIV && kind != TSPH_SOLVE_DENS) return fail(TSPH_ERR_INVALID, "unknown solve kind");
+    if (kind == TSPH_SOLVE_DIV && c->kl_phase != 2)
+        return kl_state(what, "the divergence solve runs between tsph_density_alpha and tsph_nonpressure");
+    if (kind == TSPH_SOLVE_DENS && c->kl_phase != 3)
+        return kl_state(what, "the density solve runs between tsph_nonpressure and the weakly compressible, "
+                              "volume-fraction or update calls");
+    return TSPH_OK;
+}
+
+int tsph_adv_psi(tsph_ctx *c, int kind, double *compression_out, void *stream) {
+    int rc = kl_check(c, "tsph_adv_psi");
+    if (rc) return rc;
+    rc = kl_solve_phase(c, kind, "tsph_adv_psi");
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    launch_psi(*c, st, 1);
+    TSPH_CK(cudaGetLastError());
+    c->kl_psi = 1;
+    if (compression_out) {
+        rc = kl_read_step(c, st);
+        if (rc) return rc;
+        *compression_out = c->host_ss[0].psi_sum / (double)c->host_sc[0].f_n;
+    }
+    return TSPH_OK;
+}
+
+int tsph_update_vel_adv(tsph_ctx *c, int kind, void *stream) {
+    int rc = kl_check(c, "tsph_update_vel_adv");
+    if (rc) return rc;
+    rc = kl_solve_phase(c, kind, "tsph_update_vel_adv");
+    if (rc) return rc;
+    if (!c->kl_psi) return kl_state("tsph_update_vel_adv", "each sweep B follows a sweep A (tsph_adv_psi)");
+    launch_vel(*c, kind == TSPH_SOLVE_DIV ? kSolveDiv : kSolveDens, 0, 0, (cudaStream_t)stream, 1);
+    TSPH_CK(cudaGetLastError());
+    c->kl_psi = 0;
+    return TSPH_OK;
+}
+
+int tsph_solve(tsph_ctx *c, int kind, double tol, int32_t it_min, int32_t it_max, int32_t *it_out, double *err_out,
+               void *stream) {
+    int rc = kl_check(c, "tsph_solve");
+    if (rc) return rc;
+    rc = kl_solve_phase(c, kind, "tsph_solve");
+    if (rc) return rc;
+    const SceneConst &h = c->host_sc[0];
+    if (tol < 0.0) tol = kind == TSPH_SOLVE_DIV ? (double)h.div_tol : (double)h.comp_tol;
+    if (it_min < 0) it_min = h.iter_min;
+    if (it_max < 0) it_max = h.iter_max;
+    cudaStream_t st = (cudaStream_t)stream;
+    // the compression the first loop test reads: the last solve's (main.py:201, 222)
+    rc = kl_read_step(c, st);
+    if (rc) return rc;
+    double comp = c->host_sp[0].compression;
+    int it = 0;
+    const int dk = kind == TSPH_SOLVE_DIV ? kSolveDiv : kSolveDens;
+    while (it < it_min || comp > tol) {
+        launch_psi(*c, st, 1);
+        launch_vel(*c, dk, 0, 0, st, 1);
+        TSPH_CK(cudaGetLastError());
+        rc = kl_read_step(c, st);
+        if (rc) return rc;
+        comp = c->host_sp[0].compression;
+        ++it;
+        if (it > it_max) {
+            launch_status_or(*c, kind == TSPH_SOLVE_DIV ? TSPH_ST_DIV_ITER_CAP : TSPH_ST_DENS_ITER_CAP, st);
+            break;
+        }
+    }
+    c->kl_psi = 0;
+    if (it_out) *it_out = it;
+    if (err_out) *err_out = comp;
+    TSPH_CK(cudaGetLastError());
+    return TSPH_OK;
+}
+
+int tsph_nonpressure(tsph_ctx *c, int32_t terms, void *stream) {
+    int rc = kl_check(c, "tsph_nonpressure");
+    if (rc) return rc;
+    if (c->kl_phase != 2) return kl_state("tsph_nonpressure", "it follows tsph_density_alpha and the divergence solve");
+    if (terms & ~TSPH_TERM_ALL) return fail(TSPH_ERR_INVALID, "tsph_nonpressure: unknown TSPH_TERM_* bits");
+    cudaStream_t st = (cudaStream_t)stream;
+    launch_advect(*c, st, terms);
+    launch_solve_begin(*c, kSolveDens, 0, 0, st);  // the predicted v_adv starts the density solve
+    TSPH_CK(cudaGetLastError());
+    c->kl_phase = 3;
+    c->kl_psi = 0;
+    return TSPH_OK;
+}
+
+int tsph_wc_pressure(tsph_ctx *c, const tsph_set *b, void *stream) {
+    int rc = kl_check(c, "tsph_wc_pressure");
+    if (rc) return rc;
+    if (!b) return fail(TSPH_ERR_INVALID, "null argument");
+    if (!c->p.wcsph_enabled) return fail(TSPH_ERR_INVALID, "tsph_wc_pressure: the context has wcsph_enabled = 0");
+    if (c->kl_phase != 3) return kl_state("tsph_wc_pressure", "it follows the density solve");
+    launch_wc(*c, *b, (cudaStream_t)stream);
+    TSPH_CK(cudaGetLastError());
+    c->kl_phase = 4;
+    return TSPH_OK;
+}
+
+int tsph_fbm_pass(tsph_ctx *c, int32_t *general_flag_out, void *stream) {
+    int rc = kl_check(c, "tsph_fbm_pass");
+    if (rc) return rc;
+    if (!c->p.fbm_enabled) return fail(TSPH_ERR_INVALID, "tsph_fbm_pass: the context has fbm_enabled = 0");
+    if (c->kl_phase < 3 || c->kl_phase > 5)
+        return kl_state("tsph_fbm_pass", "the volume-fraction loop follows the density solve");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!c->kl_fbm) {
+        launch_fbm_begin(*c, 0, 0, st);
+        c->kl_fbm = 1;
+    }
+    launch_fbm_pass(*c, 0, 0, st);
+    TSPH_CK(cudaGetLastError());
+    c->kl_phase = 5;
+    rc = kl_read_step(c, st);
+    if (rc) return rc;
+    if (general_flag_out) *general_flag_out = c->host_ss[0].gflag_out;
+    return TSPH_OK;
+}
+
+int tsph_update(tsph_ctx *c, const tsph_set *f, const tsph_set *b, void *stream) {
+    int rc = kl_check(c, "tsph_update");
+    if (rc) return rc;
+    if (c->kl_phase < 2) return kl_state("tsph_update", "it ends a step begun by tsph_grid_build and tsph_density_alpha");
+    rc = bind_sets(c, f, b);
+    if (rc) return rc;
+    launch_unsort(*c, *f, *b, (cudaStream_t)stream);
+    TSPH_CK(cudaGetLastError());
+    c->kl_phase = 0;
+    c->stepped++;
+    return TSPH_OK;
 }
 
 int tsph_read_scene_stats(tsph_ctx *c, int first, int count, tsph_stats *out, void *stream) {

@@ -180,6 +180,7 @@ struct FluidBuf {
     float4 *pos;       // x, y, z, X (mass for DFSPH, rest_volume for VFSPH)
     float2 *mv;        // mass, rest_volume
     float4 *mpsi;      // mass, psi (sph_psi), psi0 (rest_psi), alpha
+    float *psilo;      // low part of psi: psi + psilo is the density sweep's compensated sum
     float *rho0;       // rest_density
     float4 *vel;       // velocity after the divergence solve
     float4 *vadv;      // two buffers of cap: v_adv ping-pong

@@ -31,6 +31,14 @@ struct tsph_ctx {
     // second stream for the boundary set's share of a phase (fork_side / join_side)
     cudaStream_t side;
     cudaEvent_t ev_fork, ev_join;
+    // kernel-level composition (tsph_grid_build ... tsph_update): how far the
+    // step has got (0: none in progress, 1 grid built, 2 density done, 3
+    // non-pressure forces done, 4 weakly compressible block done, 5 in the
+    // volume-fraction loop), whether a sweep A awaits its sweep B, and whether
+    // the volume-fraction loop has begun
+    int kl_phase, kl_psi, kl_fbm;
+    // particle capacities given at create (the caller-order tables are this long)
+    int64_t cap_f, cap_b;
 };
 
 namespace tsph {
@@ -55,9 +63,13 @@ void launch_density(tsph_ctx &c, cudaStream_t st);
 void launch_clear_psi_ready(tsph_ctx &c, cudaStream_t st);
 void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
 void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
-void launch_psi(tsph_ctx &c, cudaStream_t st);
-void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st);
-void launch_advect(tsph_ctx &c, cudaStream_t st);
+// force = 1: the host runs the solver loop (kernel-level calls); see k_psi / k_vel
+void launch_psi(tsph_ctx &c, cudaStream_t st, int force = 0);
+void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st, int force = 0);
+// terms: TSPH_TERM_* bits of the non-pressure forces to apply
+void launch_advect(tsph_ctx &c, cudaStream_t st, int terms = TSPH_TERM_ALL);
+// ORs status bits into scene 0's step status (host-driven loops that hit their cap)
+void launch_status_or(tsph_ctx &c, int bits, cudaStream_t st);
 
 // wcsph.cu
 void launch_wc(tsph_ctx &c, const tsph_set &b, cudaStream_t st);

@@ -49,6 +49,21 @@ __device__ __forceinline__ void publish_any(const KConst &k, int SceneStep::*fie
 }
 
 // ----------------------------------------------------------------------------- density
+// s + e accumulates a sum with the rounding error of every addition kept in e
+// (Knuth's TwoSum, exact for any order of the terms).  The density sweep sums
+// the fluid's density and compression this way: psi - psi0, which the pressure
+// solves start from, cancels all but ~1e-3 (DFSPH) or ~1e-6 (VFSPH) of psi, so
+// an FP32 sum's own rounding (a few 1e-7 of psi over ~40 terms) would be a
+// large part of it; with the error term the sum is exact to about one rounding
+// of psi, and psi's low part is kept beside it (FluidBuf::psilo).
+__device__ __forceinline__ void acc2(float &s, float &e, float y) {
+    const float t = __fadd_rn(s, y);
+    const float yp = __fsub_rn(t, s);
+    const float sp = __fsub_rn(t, yp);
+    e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, sp), __fsub_rn(y, yp)));
+    s = t;
+}
+
 // SPH_clean_value + SPH_prepare_attr (f,f)(f,b) + SPH_prepare_alpha_1 (f,f)(f,b)
 // + SPH_prepare_alpha_2 (f,f) + SPH_prepare_alpha (sph.py:22-38, 50-105), and the
 // neighbour list of the step.
@@ -63,7 +78,7 @@ __device__ __forceinline__ void publish_any(const KConst &k, int SceneStep::*fie
 template <int DIM, bool L = false>
 __device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf &F, float4 pi, int j, float &wsum,
                                                    float &rho, float &comp, float &a1x, float &a1y, float &a1z,
-                                                   float &a2) {
+                                                   float &a2, float &rho_e, float &comp_e) {
     const float4 pj = F.pos[j];
     float2 mv = make_float2(0.f, 0.f);
     if (L) mv = F.mv[j];
@@ -76,8 +91,8 @@ __device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf 
         const float q = r * g.inv_h;
         const float w = kw(q) * g.sig;
         wsum += w;
-        rho += w * mv.x;
-        comp += w * mv.y;
+        acc2(rho, rho_e, __fmul_rn(w, mv.x));
+        acc2(comp, comp_e, __fmul_rn(w, mv.y));
         if (L || r2 > 0.f) {
             const float wg = kwg(q) * g.sig_h;
             const float f = pj.w * wg * ri;
@@ -91,7 +106,8 @@ __device__ __forceinline__ void density_pair_fluid(const Geo &g, const FluidBuf 
 
 template <int DIM, bool L = false>
 __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf &B, float4 pi, int j, float &wsum,
-                                                   float &rho, float &comp, float &a1x, float &a1y, float &a1z) {
+                                                   float &rho, float &comp, float &a1x, float &a1y, float &a1z,
+                                                   float &rho_e, float &comp_e) {
     const float4 pj = B.pos[j];
     float2 mv = make_float2(0.f, 0.f);
     if (L) mv = B.mv[j];
@@ -104,8 +120,8 @@ __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf 
         const float q = r * g.inv_h;
         const float w = kw(q) * g.sig;
         wsum += w;
-        rho += w * mv.x;
-        comp += w * mv.y;
+        acc2(rho, rho_e, __fmul_rn(w, mv.x));
+        acc2(comp, comp_e, __fmul_rn(w, mv.y));
         if (L || r2 > 0.f) {
             const float f = pj.w * kwg(q) * g.sig_h * ri;
             a1x += f * dx;
@@ -113,6 +129,39 @@ __device__ __forceinline__ void density_pair_bound(const Geo &g, const BoundBuf 
             a1z += f * dz;
         }
     }
+}
+
+// Sums of the density sweep for one fluid particle.
+struct DensAcc {
+    float wsum, rho, comp, a2, a1x, a1y, a1z, pacc, rho_e, comp_e;
+};
+
+// One recorded pair (0 < r < h known) of the density sweep's list pass: the
+// density and alpha terms and, with P0, k_psi's pair term for the divergence
+// solve's first iteration -- one distance, one reciprocal square root and one
+// spline gradient serve all of them.  The gradient factor is formed in k_psi's
+// order, ((W'(q) sig / h) / r) X_j, so the psi term is k_psi's bit for bit.
+// FLUIDJ: the neighbour is a fluid particle (alpha_2 has no boundary term,
+// main.py:194-195).
+template <bool FLUIDJ, bool P0>
+__device__ __forceinline__ void density_list_pair(const Geo &g, float4 pi, float4 pj, float2 mv, float4 vi,
+                                                  float4 vj, DensAcc &a) {
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    float r;
+    const float ri = pair_rinv_pos(r2, r);
+    const float q = r * g.inv_h;
+    const float w = kw(q) * g.sig;
+    a.wsum += w;
+    acc2(a.rho, a.rho_e, __fmul_rn(w, mv.x));
+    acc2(a.comp, a.comp_e, __fmul_rn(w, mv.y));
+    const float wg = kwg(q) * g.sig_h;
+    const float f = wg * ri * pj.w;
+    a.a1x += f * dx;
+    a.a1y += f * dy;
+    a.a1z += f * dz;
+    if (FLUIDJ) a.a2 += __fdividef(wg * wg * pj.w * pj.w, mv.x);
+    if (P0) a.pacc += f * (dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z));
 }
 
 // In the one-scene instance the divergence solve's first psi sweep (k_psi's
@@ -145,7 +194,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
         const float4 vi = psi0 ? vin[s] : make_float4(0.f, 0.f, 0.f, 0.f);
         bool ok;
         const long long code = cell_code<DIM>(pi, g, ok);
-        float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f, pacc = 0.f;
+        float wsum = 0.f, rho = 0.f, comp = 0.f, a2 = 0.f, pacc = 0.f, rho_e = 0.f, comp_e = 0.f;
         float a1x = 0.f, a1y = 0.f, a1z = 0.f;
         int nfl = 0, nbo = 0;
         int *L = F.nbr;
@@ -190,8 +239,8 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
                     } else {
                         const float2 mv = F.mv[j];
                         wsum += w0;
-                        rho += w0 * mv.x;
-                        comp += w0 * mv.y;
+                        acc2(rho, rho_e, __fmul_rn(w0, mv.x));
+                        acc2(comp, comp_e, __fmul_rn(w0, mv.y));
                     }
                 }
             });
@@ -206,32 +255,35 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
                     } else {
                         const float2 mv = B.mv[j];
                         wsum += w0;
-                        rho += w0 * mv.x;
-                        comp += w0 * mv.y;
+                        acc2(rho, rho_e, __fmul_rn(w0, mv.x));
+                        acc2(comp, comp_e, __fmul_rn(w0, mv.y));
                     }
                 }
             });
             nbo = nrec - nfl;
             if (nfl + nbo <= cap) {
                 // phase 2: the arithmetic over the recorded pairs
-                walk_blocks<1, false>(F.nbr, s, stride, 0, nfl, nfl + nbo,
-                    [&](int j) {
-                        density_pair_fluid<DIM, true>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
-                        if (psi0) psi_pair(F.pos, vin, j, std::true_type{});
-                    },
-                    [&](int j) {
-                        density_pair_bound<DIM, true>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z);
-                        if (psi0) psi_pair(B.pos, B.vadv, j, std::true_type{});
-                    });
+                DensAcc a = {wsum, rho, comp, 0.f, 0.f, 0.f, 0.f, 0.f, rho_e, comp_e};
+                if (psi0) {
+                    walk_blocks<1, false>(F.nbr, s, stride, 0, nfl, nfl + nbo,
+                        [&](int j) { density_list_pair<true, true>(g, pi, F.pos[j], F.mv[j], vi, vin[j], a); },
+                        [&](int j) { density_list_pair<false, true>(g, pi, B.pos[j], B.mv[j], vi, B.vadv[j], a); });
+                } else {
+                    walk_blocks<1, false>(F.nbr, s, stride, 0, nfl, nfl + nbo,
+                        [&](int j) { density_list_pair<true, false>(g, pi, F.pos[j], F.mv[j], vi, vi, a); },
+                        [&](int j) { density_list_pair<false, false>(g, pi, B.pos[j], B.mv[j], vi, vi, a); });
+                }
+                wsum = a.wsum; rho = a.rho; comp = a.comp; a2 = a.a2; pacc = a.pacc;
+                a1x = a.a1x; a1y = a.a1y; a1z = a.a1z; rho_e = a.rho_e; comp_e = a.comp_e;
             } else {
                 // list overflow: one scan with the arithmetic inline
-                wsum = rho = comp = a2 = a1x = a1y = a1z = 0.f;
+                wsum = rho = comp = a2 = a1x = a1y = a1z = rho_e = comp_e = 0.f;
                 visit_candidates<DIM>(F.start, g, code, f_shift, 0, [&](int j) {
-                    density_pair_fluid<DIM>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2);
+                    density_pair_fluid<DIM>(g, F, pi, j, wsum, rho, comp, a1x, a1y, a1z, a2, rho_e, comp_e);
                     if (psi0) psi_pair(F.pos, vin, j, std::false_type{});
                 });
                 visit_candidates<DIM>(B.start, g, code, b_shift, 0, [&](int j) {
-                    density_pair_bound<DIM>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z);
+                    density_pair_bound<DIM>(g, B, pi, j, wsum, rho, comp, a1x, a1y, a1z, rho_e, comp_e);
                     if (psi0) psi_pair(B.pos, B.vadv, j, std::false_type{});
                 });
             }
@@ -240,16 +292,20 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
         const float4 mp = F.mpsi[s];
         float alpha = (a1x * a1x + a1y * a1y + a1z * a1z) / mp.x + a2;
         if (alpha < 1e-4f) alpha = 1e-4f;
-        F.dens[s] = make_float4(wsum, rho, comp, a2);
+        // the compensated sums rounded once; psi keeps the remainder as its low part
+        const float rho_f = __fadd_rn(rho, rho_e), comp_f = __fadd_rn(comp, comp_e);
+        const float psi = k.vfsph ? comp_f : rho_f;
+        const float psilo = k.vfsph ? __fsub_rn(comp_e, __fsub_rn(comp_f, comp)) : __fsub_rn(rho_e, __fsub_rn(rho_f, rho));
+        F.dens[s] = make_float4(wsum, rho_f, comp_f, a2);
         F.a1[s] = make_float4(a1x, a1y, a1z, 0.f);
-        const float psi = k.vfsph ? comp : rho;
+        F.psilo[s] = psilo;
         F.mpsi[s] = make_float4(mp.x, psi, mp.z, alpha);
         // psi also rides in the current v_adv's unused w (the velocity sweeps carry
         // it along), so the advection sweep gets it with the neighbour's v_adv
         F.vadv[(int64_t)st.cur * F.cap + s].w = psi;
         if (psi0) {
             // IPPE_adv_psi_init + IPPE_psi_adv_non_negative, as k_psi
-            float pa = (psi - mp.z) + pacc * k.sp[sc].dt;
+            float pa = ((psi - mp.z) + psilo) + pacc * k.sp[sc].dt;
             if (pa < 0.f) pa = 0.f;
             const float kap = pa / alpha;
             F.psiadv[s] = pa;
@@ -382,6 +438,8 @@ __global__ void k_solve_begin(KConst k, int kind, int flip, cudaGraphConditional
         st.cond = cond;
         if (kind == kSolveDiv) st.div_iter = it;
         else st.incom_iter = it;
+        // the density sweep's first-iteration psi belongs to the divergence solve
+        if (kind == kSolveDens) st.psi_ready = 0;
         if (flip) st.cur = 1 - st.cur;
         any |= cond;
     }
@@ -397,15 +455,16 @@ __global__ void k_solve_begin(KConst k, int kind, int flip, cudaGraphConditional
 // (sph.py:196-226), TPP threads per particle.  Writes psi_adv and kappa =
 // psi_adv / alpha; the scene's sum of psi_adv / psi0 goes to per-block partials
 // and, through the scene's last block, to its psi_sum (block order:
-// deterministic).
+// deterministic).  force = 1: the host runs the loop (kernel-level calls), so
+// the sweep runs whatever the device-side loop condition says.
 template <int DIM, int TPP, bool M>
-__global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBuf B, double *partials) {
+__global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBuf B, double *partials, int force) {
     __shared__ double sh[kBlock / 32];
     __shared__ unsigned int arrived;
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
     const int sc = f_block_scene<M>(k, first);
     SceneStep &st = k.ss[sc];
-    if (!st.cond) return;  // this scene's loop has ended (uniform over the block)
+    if (!st.cond && !force) return;  // this scene's loop has ended (uniform over the block)
     if (st.psi_ready) return;  // this iteration's sweep ran inside the density sweep
     if (threadIdx.x == 0) arrived = 0;
     __syncthreads();
@@ -447,7 +506,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBu
     double contrib = 0.0;
     if (act && ln.q == 0) {
         const float4 mp = F.mpsi[s];
-        float psi = (mp.y - mp.z) + acc * k.sp[sc].dt;
+        float psi = ((mp.y - mp.z) + F.psilo[s]) + acc * k.sp[sc].dt;
         if (psi < 0.f) psi = 0.f;
         const float kap = psi / mp.w;
         F.psiadv[s] = psi;
@@ -476,10 +535,12 @@ __global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBu
 // Sweep B: IPPE_update_vel_adv (f,f)(f,b), sph.py:229-244, into the scene's other
 // v_adv buffer, TPP threads per particle.  The scene's last block evaluates the
 // loop test of main.py:201-213 / 222-234 from sweep A's sum; the grid's last
-// block sets the graph's while-node condition.
+// block sets the graph's while-node condition.  force = 1 (kernel-level calls,
+// the host runs the loop): the sweep runs regardless of the device-side
+// condition and leaves the loop test and its cap to the host.
 template <int DIM, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B, int kind,
-                                                cudaGraphConditionalHandle h, int use_cond) {
+                                                cudaGraphConditionalHandle h, int use_cond, int force) {
     __shared__ unsigned int arrived;
     if (threadIdx.x == 0) arrived = 0;
     __syncthreads();
@@ -487,7 +548,7 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
     const int sc = f_block_scene<M>(k, first);
     SceneStep &st = k.ss[sc];
     const SceneConst &c = scene<M>(k, sc);
-    const bool running = st.cond != 0;
+    const bool running = force || st.cond != 0;
     if (running) {
         const Lanes<TPP> ln;
         const int64_t s = ln.s;
@@ -548,11 +609,13 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
             st.iter = it;
             if (kind == kSolveDiv) st.div_iter = it;
             else st.incom_iter = it;
-            const double tol = kind == kSolveDiv ? (double)c.div_tol : (double)c.comp_tol;
-            const int capped = it > c.iter_max;
-            const int cond = !capped && (it < c.iter_min || comp > tol);
-            if (capped) st.status |= (kind == kSolveDiv ? TSPH_ST_DIV_ITER_CAP : TSPH_ST_DENS_ITER_CAP);
-            st.cond = cond;
+            if (!force) {
+                const double tol = kind == kSolveDiv ? (double)c.div_tol : (double)c.comp_tol;
+                const int capped = it > c.iter_max;
+                const int cond = !capped && (it < c.iter_min || comp > tol);
+                if (capped) st.status |= (kind == kSolveDiv ? TSPH_ST_DIV_ITER_CAP : TSPH_ST_DENS_ITER_CAP);
+                st.cond = cond;
+            }
             st.cur = 1 - st.cur;
             st.psi_ready = 0;
             st.ticket[kStVel] = 0;
@@ -611,9 +674,11 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
 // sph.py:108-166, 247-262.  The curvature term of the surface tension has no
 // kernel weight, so -- like the reference -- it runs over every candidate in the
 // template cells, not only those within h: with surface tension on this sweep
-// scans the cells; without it, it walks the neighbour list.
+// scans the cells; without it, it walks the neighbour list.  gs / vs scale the
+// gravity / viscosity terms by 1 or 0 (kernel-level calls may leave either
+// out; x * 1 is exact, so the full step's bits are unchanged).
 template <int DIM, bool ST, int TPP, bool M>
-__global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBuf B) {
+__global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBuf B, float gs, float vs) {
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
     const int sc = f_block_scene<M>(k, first);
     const SceneConst &c = scene<M>(k, sc);
@@ -713,10 +778,10 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
     if (act && ln.q == 0) {
         float4 *vout = F.vadv + (1 - cur) * F.cap;
         const float dt = k.sp[sc].dt;
-        const float mu = c.mu / F.rho0[s];
-        const float ax = c.g[0] + vx * mu + sx;
-        const float ay = c.g[1] + vy * mu + sy;
-        const float az = (DIM == 3 ? c.g[2] : 0.f) + vz * mu + sz;
+        const float mu = (c.mu * vs) / F.rho0[s];
+        const float ax = c.g[0] * gs + vx * mu + sx;
+        const float ay = c.g[1] * gs + vy * mu + sy;
+        const float az = (DIM == 3 ? c.g[2] * gs : 0.f) + vz * mu + sz;
         F.acc[s] = make_float4(ax, ay, az, 0.f);
         F.vel[s] = vi;
         vout[s] = make_float4(vi.x + ax * dt, vi.y + ay * dt, vi.z + az * dt, 0.f);
@@ -754,6 +819,10 @@ __global__ void k_clear_psi_ready(KConst k) {
 
 void launch_clear_psi_ready(tsph_ctx &c, cudaStream_t st) { k_clear_psi_ready<<<1, 256, 0, st>>>(c.k); }
 
+__global__ void k_status_or(KConst k, int bits) { atomicOr(&k.ss[0].status, bits); }
+
+void launch_status_or(tsph_ctx &c, int bits, cudaStream_t st) { k_status_or<<<1, 1, 0, st>>>(c.k, bits); }
+
 void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
     c.launches += 1;
     k_solve_begin<<<1, 256, 0, st>>>(c.k, kind, kind == kSolveDens ? 1 : 0, h, use_cond);
@@ -770,22 +839,22 @@ void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int
 
 static int tpp_blocks(int64_t slots, int tpp) { return blocks_for(slots * tpp); }
 
-void launch_psi(tsph_ctx &c, cudaStream_t st) {
+void launch_psi(tsph_ctx &c, cudaStream_t st, int force) {
     c.launches += 1;
     const int tpp = c.tpp;
     const int nb = tpp_blocks(c.F.cap, tpp);
     TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
-        if (c.k.dim == 3) k_psi<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
-        else k_psi<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials)))
+        if (c.k.dim == 3) k_psi<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials, force);
+        else k_psi<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials, force)))
 }
 
-void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
+void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st, int force) {
     c.launches += 1;
     const int tpp = c.tpp;
     const int nb = tpp_blocks(c.F.cap, tpp);
     TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
-        if (c.k.dim == 3) k_vel<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond);
-        else k_vel<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond)))
+        if (c.k.dim == 3) k_vel<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond, force);
+        else k_vel<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond, force)))
 }
 
 void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
@@ -793,25 +862,26 @@ void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int 
     launch_vel(c, kind, h, use_cond, st);
 }
 
-void launch_advect(tsph_ctx &c, cudaStream_t st) {
+void launch_advect(tsph_ctx &c, cudaStream_t st, int terms) {
     const int tpp = c.tpp;
     const int nb = tpp_blocks(c.F.cap, tpp);
-    const bool st_on = c.st_on != 0;
+    const bool st_on = c.st_on != 0 && (terms & TSPH_TERM_SURFACE_TENSION);
+    const float gs = (terms & TSPH_TERM_GRAVITY) ? 1.f : 0.f, vs = (terms & TSPH_TERM_VISCOSITY) ? 1.f : 0.f;
     c.launches += st_on ? 2 : 1;
     TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
         if (c.k.dim == 3) {
             if (st_on) {
                 k_normal<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
-                k_advect<3, true, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<3, true, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, gs, vs);
             } else {
-                k_advect<3, false, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<3, false, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, gs, vs);
             }
         } else {
             if (st_on) {
                 k_normal<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
-                k_advect<2, true, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<2, true, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, gs, vs);
             } else {
-                k_advect<2, false, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
+                k_advect<2, false, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, gs, vs);
             }
         }))
 }

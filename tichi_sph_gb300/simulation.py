@@ -187,7 +187,7 @@ class Simulation:
     def solver(self):
         if self._solver is None:
             self._solver = Solver(self.config, self.fluid, self.bound, fbm=self.fbm, use_graph=self.use_graph,
-                                  wcsph=self.wcsph)
+                                  wcsph=self.wcsph, ngrid=self.ngrid)
         return self._solver
 
     # ---------------------------------------------------------------- scenario

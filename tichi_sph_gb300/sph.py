@@ -5,6 +5,47 @@
 the C ABI (``tsph_sph_step`` / ``tsph_substep``), replayed as a CUDA graph with
 device-side solver loops.  :class:`Solver` owns the context; the module-level
 ``cfl_condition`` / ``sph_step`` mirror the reference's entry points.
+
+Kernel-level composition.  The module-level functions named after the
+reference's kernels (``SPH_prepare_attr(ngrid, obj, nobj)``, ``IPPE_adv_psi``,
+``IPPE_update_vel_adv``, ``SPH_advection_*``, ``SPH_FBM_*``, ``SPH_update_*``,
+...) let a caller write ``sph_step`` as ``main.py:175-256`` does, with its own
+Python solver loops reading ``fluid.compression[None]``.  The CUDA path fuses
+the reference's kernels into a few sweeps, so the calls are gathered into the
+groups those sweeps compute, and a group runs (one C call) when its last call
+arrives:
+
+=================================================  =======================  ==========================
+reference calls (main.py order)                    C entry                  runs at
+=================================================  =======================  ==========================
+``ngrid.clear_node/encode/mem_shift/fill_node``,    ``tsph_grid_build``      the last of the eight
+``SPH_clean_value`` (fluid, bound)
+``SPH_prepare_attr`` x4, ``_alpha_1`` x2,           ``tsph_density_alpha``   the last of the ten
+``_alpha_2`` x2, ``_alpha`` x2
+``SPH_vel_2_vel_adv``                               (part of the gather)     --
+``IPPE_adv_psi_init``, ``IPPE_adv_psi`` (f,f)(f,b), ``tsph_adv_psi``         the last of the four; sets
+``IPPE_psi_adv_non_negative``                                                ``fluid.compression[None]``
+``IPPE_update_vel_adv`` (f,f)(f,b)                  ``tsph_update_vel_adv``  the second
+``SPH_vel_adv_2_vel``, gravity / viscosity /        ``tsph_nonpressure``     ``SPH_advection_update_
+surface tension (each optional),                                             vel_adv``
+``SPH_advection_update_vel_adv``
+``WC_pressure_val``, ``WC_pressure_acce`` (f,f)     ``tsph_wc_pressure``     ``SPH_advection_update_
+(f,b), ``SPH_advection_update_vel_adv``                                      vel_adv``
+``SPH_FBM_clean_tmp/convect/diffuse/check_tmp``     ``tsph_fbm_pass``        the last of the four; sets
+                                                                             ``fluid.general_flag[None]``
+``SPH_update_volume_frac`` (with the volume-        ``tsph_update``          the last of the group;
+fraction update), ``SPH_update_mass/pos/energy``                             refreshes the scalars
+=================================================  =======================  ==========================
+
+A Jacobi iteration belongs to the divergence solve before the non-pressure
+group and to the density solve after it.  A group left incomplete when a call
+of another group arrives raises :class:`~tichi_sph_gb300._native.TsphError`
+naming what is missing: each fused sweep computes all of its group's pair terms
+(e.g. a density sweep without the fluid-boundary pairs does not exist).
+Between ``tsph_grid_build`` and ``tsph_update`` the step's state lives in the
+context; the particle arrays hold the previous step's values until the update
+group has run.  A step composed in ``main.py``'s order equals the fused
+``sph_step`` bit for bit (the same kernels in the same order).
 """
 import torch
 
@@ -25,7 +66,8 @@ class Solver:
     host-driven, reading the convergence value every iteration as the reference
     does (``main.py:201,222``)."""
 
-    def __init__(self, config, fluid, bound, fbm=False, use_graph=True, fbm_max_passes=1000, wcsph=False):
+    def __init__(self, config, fluid, bound, fbm=False, use_graph=True, fbm_max_passes=1000, wcsph=False,
+                 ngrid=None):
         if fluid.device.type != "cuda" or bound.device.type != "cuda":
             raise RuntimeError("tichi_sph_gb300: particle sets must live on a CUDA device")
         self.config = config
@@ -46,6 +88,13 @@ class Solver:
         self.tpp = 1
         self._stats = _native.Stats()
         self._warn = _native.StatusWarner()
+        # kernel-level composition: the reference's kernels find the solver
+        # through their particle sets and grid
+        self.composer = _Composer(self)
+        fluid._solver = self
+        bound._solver = self
+        if ngrid is not None:
+            ngrid._solver = self
 
     def set_graph_mode(self, use_graph):
         check(self._lib.tsph_set_graph_mode(self.ctx, 1 if use_graph else 0), "tsph_set_graph_mode")
@@ -102,6 +151,67 @@ class Solver:
         with torch.cuda.device(self.device):
             check(self._lib.tsph_substep(self.ctx, f, b, _native.C.c_void_p(_stream_handle(self.device))),
                   "tsph_substep")
+
+    # ------------------------------------------------------ kernel-level calls
+    def _stream(self):
+        return _native.C.c_void_p(_stream_handle(self.device))
+
+    def grid_build(self):
+        """``tsph_grid_build``: starts a step (grid, clean values, gather)."""
+        f, b = self._sets()
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_grid_build(self.ctx, f, b, self._stream()), "tsph_grid_build")
+
+    def density_alpha(self):
+        """``tsph_density_alpha``: SPH_prepare_attr / _alpha_1 / _alpha_2 / _alpha."""
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_density_alpha(self.ctx, self._stream()), "tsph_density_alpha")
+
+    def adv_psi(self, kind, read=True):
+        """``tsph_adv_psi``: one Jacobi sweep A; returns the compression if ``read``."""
+        out = _native.C.c_double(0.0)
+        ptr = _native.C.byref(out) if read else None
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_adv_psi(self.ctx, int(kind), ptr, self._stream()), "tsph_adv_psi")
+        return float(out.value) if read else None
+
+    def update_vel_adv(self, kind):
+        """``tsph_update_vel_adv``: one Jacobi sweep B."""
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_update_vel_adv(self.ctx, int(kind), self._stream()), "tsph_update_vel_adv")
+
+    def solve(self, kind, tol=-1.0, it_min=-1, it_max=-1):
+        """``tsph_solve``: a whole solver loop; returns (iterations, compression)."""
+        it = _native.C.c_int32(0)
+        err = _native.C.c_double(0.0)
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_solve(self.ctx, int(kind), float(tol), int(it_min), int(it_max),
+                                       _native.C.byref(it), _native.C.byref(err), self._stream()), "tsph_solve")
+        return int(it.value), float(err.value)
+
+    def nonpressure(self, terms=_native.TERM_ALL):
+        """``tsph_nonpressure``: the non-pressure forces selected by ``terms``."""
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_nonpressure(self.ctx, int(terms), self._stream()), "tsph_nonpressure")
+
+    def wc_pressure(self):
+        """``tsph_wc_pressure``: the weakly compressible pressure block."""
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_wc_pressure(self.ctx, _native.C.byref(self.bound.native_set()), self._stream()),
+                  "tsph_wc_pressure")
+
+    def fbm_pass(self):
+        """``tsph_fbm_pass``: one volume-fraction pass; returns general_flag."""
+        gf = _native.C.c_int32(0)
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_fbm_pass(self.ctx, _native.C.byref(gf), self._stream()), "tsph_fbm_pass")
+        return int(gf.value)
+
+    def update(self):
+        """``tsph_update``: ends the step and writes every field back."""
+        f, b = self._sets()
+        with torch.cuda.device(self.device):
+            check(self._lib.tsph_update(self.ctx, f, b, self._stream()), "tsph_update")
 
     def set_state(self, time_count=0.0, dt=0.0, compression=0.0):
         with torch.cuda.device(self.device):
@@ -180,6 +290,259 @@ class Solver:
         return fc[:nf], bc[:nb]
 
 
+class _Composer:
+    """Gathers the reference's kernel calls of a step into the groups the fused
+    sweeps compute and runs each group's C entry when its last call arrives
+    (the table in the module docstring)."""
+
+    # (name, role) -> group; roles: "f" / "b" for (obj), "ff" / "fb" / "bb" / "bf" for (obj, nobj)
+    GROUPS = {
+        "grid": {("clear_node", ""), ("encode", "f"), ("encode", "b"), ("mem_shift", ""), ("fill_node", "f"),
+                 ("fill_node", "b"), ("SPH_clean_value", "f"), ("SPH_clean_value", "b")},
+        "density": {("SPH_prepare_attr", "ff"), ("SPH_prepare_attr", "fb"), ("SPH_prepare_attr", "bb"),
+                    ("SPH_prepare_attr", "bf"), ("SPH_prepare_alpha_1", "ff"), ("SPH_prepare_alpha_1", "fb"),
+                    ("SPH_prepare_alpha_2", "ff"), ("SPH_prepare_alpha_2", "bf"), ("SPH_prepare_alpha", "f"),
+                    ("SPH_prepare_alpha", "b")},
+        "vel_2_vel_adv": {("SPH_vel_2_vel_adv", "f")},
+        "psi": {("IPPE_adv_psi_init", "f"), ("IPPE_adv_psi", "ff"), ("IPPE_adv_psi", "fb"),
+                ("IPPE_psi_adv_non_negative", "f")},
+        "vel": {("IPPE_update_vel_adv", "ff"), ("IPPE_update_vel_adv", "fb")},
+        "advection": {("SPH_vel_adv_2_vel", "f"), ("SPH_advection_update_vel_adv", "f")},
+        "wc": {("WC_pressure_val", "f"), ("WC_pressure_acce", "ff"), ("WC_pressure_acce", "fb"),
+               ("SPH_advection_update_vel_adv", "f")},
+        "fbm": {("SPH_FBM_clean_tmp", "f"), ("SPH_FBM_convect", "ff"), ("SPH_FBM_diffuse", "ff"),
+                ("SPH_FBM_check_tmp", "f")},
+        "update": {("SPH_update_mass", "f"), ("SPH_update_pos", "f"), ("SPH_update_energy", "f")},
+    }
+    # optional members: the non-pressure forces a caller may leave out
+    OPTIONAL = {"advection": {("SPH_advection_gravity_acc", "f"): _native.TERM_GRAVITY,
+                              ("SPH_advection_viscosity_acc", "ff"): _native.TERM_VISCOSITY,
+                              ("SPH_advection_surface_tension_acc", "ff"): _native.TERM_SURFACE_TENSION},
+                "update": {("SPH_update_volume_frac", "f"): 0}}
+
+    def __init__(self, solver):
+        self.solver = solver
+        self.open = None      # group being gathered
+        self.called = set()
+        self.after_advection = False
+
+    def role(self, *objs):
+        r = ""
+        for o in objs:
+            if o is self.solver.fluid:
+                r += "f"
+            elif o is self.solver.bound:
+                r += "b"
+            else:
+                raise _native.TsphError("this particle set does not belong to the solver the call reached")
+        return r
+
+    def _group_of(self, key):
+        if self.open is not None and (key in self.GROUPS[self.open] or key in self.OPTIONAL.get(self.open, {})):
+            return self.open
+        if key == ("SPH_advection_update_vel_adv", "f"):
+            return "advection"
+        for g in ("grid", "density", "vel_2_vel_adv", "psi", "vel", "advection", "fbm", "update", "wc"):
+            if key in self.GROUPS[g] or key in self.OPTIONAL.get(g, {}):
+                return g
+        raise _native.TsphError("%s%s is not a kernel of the composed step" % key)
+
+    def call(self, name, role=""):
+        key = (name, role)
+        g = self._group_of(key)
+        if self.open is not None and g != self.open:
+            missing = sorted(self.GROUPS[self.open] - self.called)
+            self.open, self.called = None, set()
+            raise _native.TsphError(
+                "composed sph_step: %s%s arrived while the %s group still lacks %s; the fused sweep of that "
+                "group computes all of them" % (name, "(" + role + ")" if role else "", g,
+                                               ", ".join("%s(%s)" % m for m in missing)))
+        if key in self.called:
+            self.open, self.called = None, set()
+            raise _native.TsphError("composed sph_step: %s(%s) called twice in one group" % key)
+        self.open = g
+        self.called.add(key)
+        if self.GROUPS[g] <= self.called:
+            called, self.open, self.called = self.called, None, set()
+            self._run(g, called)
+
+    def _run(self, g, called):
+        s = self.solver
+        fl = s.fluid
+        if g == "grid":
+            s.grid_build()
+            self.after_advection = False
+            fl.general_flag[None] = 1  # SPH_clean_value (sph.py:24)
+        elif g == "density":
+            s.density_alpha()
+        elif g == "psi":
+            kind = _native.SOLVE_DENS if self.after_advection else _native.SOLVE_DIV
+            fl.compression[None] = s.adv_psi(kind)
+        elif g == "vel":
+            s.update_vel_adv(_native.SOLVE_DENS if self.after_advection else _native.SOLVE_DIV)
+        elif g == "advection":
+            terms = 0
+            for k, bit in self.OPTIONAL["advection"].items():
+                if k in called:
+                    terms |= bit
+            s.nonpressure(terms)
+            self.after_advection = True
+        elif g == "wc":
+            s.wc_pressure()
+        elif g == "fbm":
+            fl.general_flag[None] = s.fbm_pass()
+        elif g == "update":
+            if s.fbm and ("SPH_update_volume_frac", "f") not in called:
+                raise _native.TsphError("composed sph_step: SPH_update_volume_frac(fluid) belongs to the update "
+                                        "group when the volume-fraction update is on")
+            s.update()
+            s.stats()  # statistics_*_energy, dt and compression as the reference's fields hold them
+
+
+def _composer(obj):
+    sv = getattr(obj, "_solver", None)
+    if sv is None:
+        raise _native.TsphError("no solver is bound to this particle set (create a Solver for it first)")
+    return sv.composer
+
+
+def _pair(name, obj, nobj):
+    c = _composer(obj)
+    c.call(name, c.role(obj, nobj))
+
+
+def _one(name, obj):
+    c = _composer(obj)
+    c.call(name, c.role(obj))
+
+
+# The reference's kernels (sph.py), for composing sph_step as main.py:175-256 does.
+def SPH_clean_value(obj):
+    """sph.py:22-38."""
+    _one("SPH_clean_value", obj)
+
+
+def SPH_prepare_attr(ngrid, obj, nobj):
+    """sph.py:50-64."""
+    _pair("SPH_prepare_attr", obj, nobj)
+
+
+def SPH_prepare_alpha_1(ngrid, obj, nobj):
+    """sph.py:67-81."""
+    _pair("SPH_prepare_alpha_1", obj, nobj)
+
+
+def SPH_prepare_alpha_2(ngrid, obj, nobj):
+    """sph.py:84-97."""
+    _pair("SPH_prepare_alpha_2", obj, nobj)
+
+
+def SPH_prepare_alpha(obj):
+    """sph.py:100-105."""
+    _one("SPH_prepare_alpha", obj)
+
+
+def SPH_advection_gravity_acc(obj):
+    """sph.py:108-111."""
+    _one("SPH_advection_gravity_acc", obj)
+
+
+def SPH_advection_viscosity_acc(ngrid, obj, nobj):
+    """sph.py:114-129."""
+    _pair("SPH_advection_viscosity_acc", obj, nobj)
+
+
+def SPH_advection_surface_tension_acc(ngrid, obj, nobj):
+    """sph.py:132-166."""
+    _pair("SPH_advection_surface_tension_acc", obj, nobj)
+
+
+def WC_pressure_val(obj):
+    """sph.py:169-175."""
+    _one("WC_pressure_val", obj)
+
+
+def WC_pressure_acce(ngrid, obj, nobj):
+    """sph.py:178-193."""
+    _pair("WC_pressure_acce", obj, nobj)
+
+
+def IPPE_adv_psi_init(obj):
+    """sph.py:196-199."""
+    _one("IPPE_adv_psi_init", obj)
+
+
+def IPPE_adv_psi(ngrid, obj, nobj):
+    """sph.py:202-216."""
+    _pair("IPPE_adv_psi", obj, nobj)
+
+
+def IPPE_psi_adv_non_negative(obj):
+    """sph.py:219-226: also sets ``obj.compression[None]`` (a host read, as the
+    reference's loop test makes it)."""
+    _one("IPPE_psi_adv_non_negative", obj)
+
+
+def IPPE_update_vel_adv(ngrid, obj, nobj):
+    """sph.py:229-244."""
+    _pair("IPPE_update_vel_adv", obj, nobj)
+
+
+def SPH_vel_2_vel_adv(obj):
+    """sph.py:253-256."""
+    _one("SPH_vel_2_vel_adv", obj)
+
+
+def SPH_vel_adv_2_vel(obj):
+    """sph.py:259-262."""
+    _one("SPH_vel_adv_2_vel", obj)
+
+
+def SPH_advection_update_vel_adv(obj):
+    """sph.py:247-250."""
+    _one("SPH_advection_update_vel_adv", obj)
+
+
+def SPH_update_pos(obj):
+    """sph.py:265-269."""
+    _one("SPH_update_pos", obj)
+
+
+def SPH_update_energy(obj):
+    """sph.py:272-279."""
+    _one("SPH_update_energy", obj)
+
+
+def SPH_update_mass(obj):
+    """sph.py:282-286."""
+    _one("SPH_update_mass", obj)
+
+
+def SPH_FBM_clean_tmp(obj):
+    """sph.py:301-305."""
+    _one("SPH_FBM_clean_tmp", obj)
+
+
+def SPH_FBM_convect(ngrid, obj, nobj):
+    """sph.py:329-363."""
+    _pair("SPH_FBM_convect", obj, nobj)
+
+
+def SPH_FBM_diffuse(ngrid, obj, nobj):
+    """sph.py:308-326."""
+    _pair("SPH_FBM_diffuse", obj, nobj)
+
+
+def SPH_FBM_check_tmp(obj):
+    """sph.py:366-372."""
+    _one("SPH_FBM_check_tmp", obj)
+
+
+def SPH_update_volume_frac(obj):
+    """sph.py:375-379."""
+    _one("SPH_update_volume_frac", obj)
+
+
 def fp32_fma_peak(device=None):
     """FP32 FMA rate of the GPU in TFLOP/s (independent FMA chains on every SM)."""
     dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
@@ -195,9 +558,9 @@ def map_velocity(solver, grid):
     solver.map_velocity(grid)
 
 
-def cfl_condition(solver):
-    """Module-level form of ``cfl_condition(fluid)`` (sph.py:41-47)."""
-    solver.cfl_condition()
+def cfl_condition(obj):
+    """``cfl_condition(fluid)`` (sph.py:41-47): takes the fluid set (or its Solver)."""
+    (obj if isinstance(obj, Solver) else _composer(obj).solver).cfl_condition()
 
 
 def sph_step(solver):

@@ -200,20 +200,42 @@ def _np_normalize(v):
 
 
 class Ngrid:
-    """Cell-grid view in the reference's layout (``sph_obj.py:281-323``).
+    """The reference's neighbour grid, ``sph_obj.py:281-323``.
 
-    The CUDA path keeps one sorted grid per particle set; :meth:`from_solver`
-    assembles the reference's combined arrays (``node_part_count``,
-    ``node_part_shift``, ``part_pid_in_node``, ``part_uid_in_node``) from them,
-    with each cell holding its fluid particles, then its boundary particles, in
-    particle order -- one of the layouts the reference's atomics can produce."""
+    The cell grids themselves live inside the solver's CUDA context (one sorted
+    grid per particle set, built every step).  The methods below are the
+    reference's calls as ``main.py:178-183`` makes them; with a solver bound
+    (``Solver(..., ngrid=ngrid)``, which :class:`~tichi_sph_gb300.simulation.Simulation`
+    does) they take part in a step composed from the reference's kernels, see
+    :mod:`tichi_sph_gb300.sph`: the grid is built once all six calls and both
+    ``SPH_clean_value`` calls of the step have been made."""
 
     def __init__(self, config):
         self.config = config
-        self.node_part_count = None
-        self.node_part_shift = None
-        self.part_pid_in_node = None
-        self.part_uid_in_node = None
+        self._solver = None
+
+    def _composer(self):
+        if self._solver is None:
+            raise RuntimeError("Ngrid: no solver is bound to this grid (create the Solver with ngrid=...)")
+        return self._solver.composer
+
+    def clear_node(self):
+        """``Ngrid.clear_node``, sph_obj.py:295-298."""
+        self._composer().call("clear_node")
+
+    def encode(self, obj):
+        """``Ngrid.encode``, sph_obj.py:300-306."""
+        c = self._composer()
+        c.call("encode", c.role(obj))
+
+    def mem_shift(self):
+        """``Ngrid.mem_shift``, sph_obj.py:308-314."""
+        self._composer().call("mem_shift")
+
+    def fill_node(self, obj):
+        """``Ngrid.fill_node``, sph_obj.py:316-323."""
+        c = self._composer()
+        c.call("fill_node", c.role(obj))
 
 
 class Grid:
