@@ -42,7 +42,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.environ.get("TICHI_REFERENCE", "")
 SCENES = os.path.join(HERE, "scenes")
 STEPS = {"dfsph2d": 3, "dfsph2d_r2": 2, "dfsph3d": 2, "vfsph2d": 3, "vfsph3d": 2, "edge2d": 2,
-         "wcsph2d": 3, "wcsph3d": 2}
+         "wcsph2d": 3, "wcsph3d": 2, "inlet3d": 8}
+# scenes whose scenario emits at run time (an inlet, objects with a "time"):
+# each substep starts with the reference's refresh_scenario (main.py:346)
+EMIT_SCENES = {"inlet3d"}
 FBM_SCENES = {"vfsph2d", "vfsph3d"}
 WC_SCENES = {"wcsph2d", "wcsph3d"}
 VF_NOISE_SEED = 3
@@ -72,21 +75,9 @@ def _child(scene, mode):
     fluid = R.Fluid(max_part_num=config.fluid_max_part_num[None])
     bound = R.Fluid(max_part_num=config.bound_max_part_num[None])
     objs = {"fluid": fluid, "bound": bound}
-    # init_scenario / add_to_scenario, main.py:42-79 (cube and box only)
-    for part in R.scenario_buffer:
-        if part == "sim_env":
-            continue
-        for param in R.scenario_buffer[part]["objs"]:
-            obj = objs[part]
-            if param["type"] == "cube":
-                obj.scene_add_cube(param["start_pos"], param["end_pos"], param["volume_frac"],
-                                   param["vel"], int(param["color"], 16), param["particle_relaxing_factor"])
-            elif param["type"] == "box":
-                obj.scene_add_box(param["start_pos"], param["end_pos"], param["layers"],
-                                  param["volume_frac"], param["vel"], int(param["color"], 16),
-                                  param["particle_relaxing_factor"])
-            else:
-                raise RuntimeError("golden scenes use cube/box objects only")
+    gv = R.GlobalVariable()
+    scenario = _Scenario(R, config, objs, gv)
+    scenario.init_scenario()
 
     if mode == "f32":
         if scene in FBM_SCENES:
@@ -117,7 +108,6 @@ def _child(scene, mode):
             arr[:n] = init[name + "_" + f]
             getattr(obj, f).from_numpy(arr)
 
-    gv = R.GlobalVariable()
     fbm = scene in FBM_SCENES
     wc = scene in WC_SCENES
     grid = _Grid(R, config) if wc else None
@@ -125,6 +115,8 @@ def _child(scene, mode):
     if grid is not None:
         rec["grid_lb"], rec["grid_dist"], rec["grid_shape"] = grid.lb, grid.dist, np.array(grid.shape)
     for step in range(STEPS[scene]):
+        if scene in EMIT_SCENES:
+            scenario.refresh_scenario()
         _substep(R, config, ngrid, fluid, bound, gv, fbm, wc, grid)
         p = "s%d_" % step
         if grid is not None:
@@ -145,6 +137,77 @@ def _child(scene, mode):
             scene, step, config.dt[None], gv.div_iter_count, gv.incom_iter_count,
             fluid.compression[None]), flush=True)
     np.savez_compressed(os.path.join(HERE, scene + ".steps.npz"), **rec)
+
+
+class _Scenario:
+    """The reference's scenario system, main.py:16-112, replayed on the reference's
+    own emitters (``scene_add_cube`` / ``scene_add_box`` / ``scene_add_from_inlet``,
+    sph_obj.py:102-163): ``main.py`` cannot be imported (it opens a window), so its
+    host-side scheduling is restated here line for line."""
+
+    def __init__(self, R, config, objs, gv):
+        self.R, self.config, self.objs, self.gv = R, config, objs, gv
+        self.wait = []     # scenario_wait_buffer, main.py:13
+        self.inlets = []   # main.py:14
+
+    def inlet_helper_get_dt(self, norm, speed, relaxing_factor):
+        """main.py:26-39."""
+        norm = np.array(norm) / np.linalg.norm(np.array(norm))
+        if speed < 0:
+            norm, speed = -norm, -speed
+        acc = np.dot(norm, self.config.gravity.to_numpy())
+        r = self.config.part_size[1]
+        if acc < 1e-6:
+            return r * relaxing_factor / speed if speed > 0 else float("inf")
+        return ((speed ** 2 + 2 * acc * r) ** 0.5 - speed) / acc * relaxing_factor
+
+    def add_to_scenario(self, part, param):
+        """main.py:42-60 (cube, box, inlet)."""
+        obj = self.objs[part]
+        t = param["type"]
+        if t == "cube":
+            obj.scene_add_cube(param["start_pos"], param["end_pos"], param["volume_frac"], param["vel"],
+                               int(param["color"], 16), param["particle_relaxing_factor"])
+        elif t == "box":
+            obj.scene_add_box(param["start_pos"], param["end_pos"], param["layers"], param["volume_frac"],
+                              param["vel"], int(param["color"], 16), param["particle_relaxing_factor"])
+        elif t == "inlet":
+            param["obj"] = part
+            param["dt"] = self.inlet_helper_get_dt(param["norm"], param["speed"], param["particle_relaxing_factor"])
+            param["t_pre"] = self.gv.time_count - param["dt"]
+            self.inlets.append(param)
+        else:
+            raise RuntimeError("golden scenes use cube, box and inlet objects")
+
+    def init_scenario(self):
+        """main.py:62-74."""
+        for part in self.R.scenario_buffer:
+            if part == "sim_env":
+                continue
+            for param in self.R.scenario_buffer[part]["objs"]:
+                if "time" not in param or param["time"] <= 0.0:
+                    self.add_to_scenario(part, param)
+                else:
+                    param["_part"] = part
+                    self.wait.append(param)
+
+    def refresh_scenario(self):
+        """main.py:81-112 (refresh_inlets after the delayed objects)."""
+        gv = self.gv
+        for i in range(len(self.wait) - 1, -1, -1):
+            param = self.wait[i]
+            if param["time"] <= gv.time_count:
+                self.add_to_scenario(param["_part"], param)
+                self.wait.pop(i)
+        for i in range(len(self.inlets) - 1, -1, -1):
+            inlet = self.inlets[i]
+            if "end_time" in inlet and gv.time_count >= inlet["end_time"]:
+                self.inlets.pop(i)
+            elif gv.time_count >= inlet["t_pre"] + inlet["dt"]:
+                inlet["t_pre"] = gv.time_count
+                self.objs[inlet["obj"]].scene_add_from_inlet(
+                    inlet["center"], inlet["size"], inlet["norm"], inlet["speed"], inlet["volume_frac"],
+                    int(inlet["color"], 16), inlet["particle_relaxing_factor"])
 
 
 class _Grid:
