@@ -8,7 +8,9 @@
  * kernel of sph.py, each pair kernel scanning the (2r+1)^d template cells and
  * filtering by uid (sph.py:52-60), and the host-driven solver loops of
  * main.py:175-256.  REAL is float (the reference's default_fp=f32; the CPU
- * baseline) or double (a mid-size FP64 oracle).  OpenMP parallelises the
+ * baseline) or double (the FP64 oracle: every field, sum and pair term in
+ * double; the FP32 particle arrays are converted to double working arrays at
+ * the start of a substep and back at its end).  OpenMP parallelises the
  * outermost particle loop of every kernel, as Taichi's CPU backend does.
  */
 #include <math.h>
@@ -42,12 +44,26 @@ typedef struct {
     int32_t div_iter, incom_iter, fbm_passes;
 } port_stats;
 
-/* one particle set: tsph_set host pointers + uid and the solver aliases */
+/* the fields of one particle set (the tsph_set fields) in REAL */
 typedef struct {
-    tsph_set *s;
+    int64_t n;
+    REAL *pos, *vel, *vel_adv, *acce, *acce_adv;
+    REAL *mass, *rest_density, *rest_volume;
+    REAL *volume_frac, *volume_frac_tmp;
+    REAL *W, *sph_density, *sph_compression, *psi_adv;
+    REAL *alpha, *alpha_1, *alpha_2;
+    REAL *normal, *drift_vel, *fbm_zeta;
+    REAL *pressure;
+    int32_t *flag;
+    int32_t *neighb_cell_seq, *neighb_in_cell_seq, *neighb_cell_structured_seq;
+} rset;
+
+/* one particle set: its fields + uid and the solver aliases */
+typedef struct {
+    rset *s;
     int uid;
-    float *X, *psi; /* X = mass | rest_volume; sph_psi = sph_density | sph_compression */
-    float *rest_psi; /* NULL means the `ones` field (VFSPH) */
+    REAL *X, *psi; /* X = mass | rest_volume; sph_psi = sph_density | sph_compression */
+    REAL *rest_psi; /* NULL means the `ones` field (VFSPH) */
     double compression, ke, pe;
     int general_flag;
 } obj_t;
@@ -87,11 +103,11 @@ static int64_t code_of(const port_ctx *c, const int32_t *st) {
 static void clear_node(port_ctx *c) { memset(c->node_part_count, 0, sizeof(int32_t) * c->p.node_num); }
 
 static void encode(port_ctx *c, obj_t *o) {
-    tsph_set *s = o->s;
+    rset *s = o->s;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < s->n; ++i) {
         for (int d = 0; d < D; ++d) {
-            float f = floorf((s->pos[i * D + d] - c->p.lb[d]) / c->p.kernel_h);
+            float f = floorf(((float)s->pos[i * D + d] - c->p.lb[d]) / c->p.kernel_h);
             s->neighb_cell_structured_seq[i * D + d] = (int32_t)f;
         }
         int64_t code = code_of(c, s->neighb_cell_structured_seq + i * D);
@@ -113,7 +129,7 @@ static void mem_shift(port_ctx *c) {
 }
 
 static void fill_node(port_ctx *c, obj_t *o) {
-    tsph_set *s = o->s;
+    rset *s = o->s;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < s->n; ++i) {
         int32_t code = s->neighb_cell_seq[i];
@@ -156,7 +172,7 @@ static void fill_node(port_ctx *c, obj_t *o) {
 
 /* ---------------------------------------------------------------- sph.py */
 static void clean_value(port_ctx *c, obj_t *o) {
-    tsph_set *s = o->s;
+    rset *s = o->s;
     o->general_flag = 1;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < s->n; ++i) {
@@ -170,7 +186,7 @@ static void clean_value(port_ctx *c, obj_t *o) {
 
 static void cfl_condition(port_ctx *c, obj_t *o) {
     REAL dt = (REAL)c->p.part_size / (REAL)c->p.cs;
-    tsph_set *s = o->s;
+    rset *s = o->s;
     for (int64_t i = 0; i < s->n; ++i) {
         REAL v2 = 0;
         for (int d = 0; d < D; ++d) v2 += (REAL)s->vel[i * D + d] * (REAL)s->vel[i * D + d];
@@ -283,7 +299,9 @@ static void surface_tension_acc(port_ctx *c, obj_t *o, obj_t *no) {
         REAL a[3] = {0, 0, 0};
         FOR_NEIGHBOURS(c, o, no, i, j, {
             XIJ(o, no, i, j, x, r);
-            if (r > 0 && o->s->volume_frac[i * P] > (REAL)0.99 && no->s->volume_frac[j * P] > (REAL)0.99) {
+            /* sph.py:163 compares an f32 field with a literal that Taichi's default_fp=f32
+             * makes 0.99f; both builds compare the stored f32 values with 0.99f */
+            if (r > 0 && o->s->volume_frac[i * P] > 0.99f && no->s->volume_frac[j * P] > 0.99f) {
                 REAL coh = -gam * no->s->mass[j] * kC(c, r) / r;
                 REAL fac = 2 * rest_psi(o, i) / (o->psi[i] + no->psi[j]);
                 for (int d = 0; d < D; ++d)
@@ -345,7 +363,7 @@ static void update_vel_adv(port_ctx *c, obj_t *o, obj_t *no) {
 
 static void fbm_convect(port_ctx *c, obj_t *o, obj_t *no) {
     const REAL dt = c->dt;
-    tsph_set *s = o->s;
+    rset *s = o->s;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < s->n; ++i) {
         REAL zeta = 0;
@@ -392,7 +410,7 @@ static void fbm_convect(port_ctx *c, obj_t *o, obj_t *no) {
 
 static void fbm_diffuse(port_ctx *c, obj_t *o, obj_t *no) {
     const REAL dt = c->dt, h2 = (REAL)c->p.kernel_h2;
-    tsph_set *s = o->s;
+    rset *s = o->s;
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < s->n; ++i) {
         if (s->flag[i] != 0) continue;
@@ -412,7 +430,7 @@ static void fbm_diffuse(port_ctx *c, obj_t *o, obj_t *no) {
 
 static int fbm_check_tmp(port_ctx *c, obj_t *o) {
     int gf = 0;
-    tsph_set *s = o->s;
+    rset *s = o->s;
 #pragma omp parallel for schedule(static) reduction(| : gf)
     for (int64_t i = 0; i < s->n; ++i) {
         int neg = 0;
@@ -425,7 +443,7 @@ static int fbm_check_tmp(port_ctx *c, obj_t *o) {
 }
 
 static void update_tail(port_ctx *c, obj_t *o, int fbm) {
-    tsph_set *s = o->s;
+    rset *s = o->s;
     const REAL dt = c->dt;
     double ke = 0, pe = 0;
 #pragma omp parallel for schedule(static) reduction(+ : ke, pe)
@@ -464,7 +482,7 @@ static int solve(port_ctx *c, obj_t *f, obj_t *b, REAL tol) {
     return it;
 }
 
-static void bind(port_ctx *c, obj_t *o, tsph_set *s, int uid) {
+static void bind(port_ctx *c, obj_t *o, rset *s, int uid) {
     memset(o, 0, sizeof(*o));
     o->s = s;
     o->uid = uid;
@@ -516,8 +534,48 @@ void port_set_state(void *h, double time_count, double compression) {
 }
 
 /* run_step's substep (main.py:347-352) around sph_step (main.py:175-256). */
-int port_substep(void *h, tsph_set *fluid, tsph_set *bound, port_stats *out) {
+/* The REAL view of a tsph_set: its own arrays when REAL is float, else double
+ * copies of every field (the number of components of each: 1, dim, phases or
+ * phases x dim). */
+#define RSET_FIELDS(X_)                                                                          \
+    X_(pos, D) X_(vel, D) X_(vel_adv, D) X_(acce, D) X_(acce_adv, D) X_(mass, 1) X_(rest_density, 1) \
+    X_(rest_volume, 1) X_(volume_frac, P) X_(volume_frac_tmp, P) X_(W, 1) X_(sph_density, 1)       \
+    X_(sph_compression, 1) X_(psi_adv, 1) X_(alpha, 1) X_(alpha_1, D) X_(alpha_2, 1) X_(normal, D)  \
+    X_(drift_vel, P * D) X_(fbm_zeta, 1) X_(pressure, 1)
+
+static void rset_in(const port_ctx *c, rset *r, const tsph_set *t) {
+    r->n = t->n;
+    r->flag = t->flag;
+    r->neighb_cell_seq = t->neighb_cell_seq;
+    r->neighb_in_cell_seq = t->neighb_in_cell_seq;
+    r->neighb_cell_structured_seq = t->neighb_cell_structured_seq;
+    const int64_t n = t->n > 0 ? t->n : 1;
+#define RSET_IN(f, k)                                                                   \
+    if (sizeof(REAL) == sizeof(float)) {                                                \
+        r->f = (REAL *)t->f;                                                            \
+    } else {                                                                            \
+        r->f = (REAL *)malloc(sizeof(REAL) * (size_t)(n * (k)));                        \
+        for (int64_t i = 0; i < t->n * (k); ++i) r->f[i] = (REAL)t->f[i];              \
+    }
+    RSET_FIELDS(RSET_IN)
+#undef RSET_IN
+}
+
+static void rset_out(const port_ctx *c, rset *r, tsph_set *t) {
+    if (sizeof(REAL) == sizeof(float)) return;
+#define RSET_OUT(f, k)                                                         \
+    for (int64_t i = 0; i < t->n * (k); ++i) t->f[i] = (float)r->f[i];       \
+    free(r->f);
+    RSET_FIELDS(RSET_OUT)
+#undef RSET_OUT
+}
+
+int port_substep(void *h, tsph_set *fluid_set, tsph_set *bound_set, port_stats *out) {
     port_ctx *c = (port_ctx *)h;
+    rset fr, br;
+    rset_in(c, &fr, fluid_set);
+    rset_in(c, &br, bound_set);
+    rset *fluid = &fr, *bound = &br;
     obj_t F, B;
     bind(c, &F, fluid, 0);
     bind(c, &B, bound, 1);
@@ -532,9 +590,9 @@ int port_substep(void *h, tsph_set *fluid, tsph_set *bound, port_stats *out) {
     prepare_alpha_1(c, &F, &F); prepare_alpha_1(c, &F, &B);
     prepare_alpha_2(c, &F, &F); prepare_alpha_2(c, &B, &F);
     prepare_alpha(c, &F); prepare_alpha(c, &B);
-    memcpy(fluid->vel_adv, fluid->vel, sizeof(float) * fluid->n * D);
+    memcpy(fluid->vel_adv, fluid->vel, sizeof(REAL) * fluid->n * D);
     int kd = solve(c, &F, &B, (REAL)c->p.divergence_threshold);
-    memcpy(fluid->vel, fluid->vel_adv, sizeof(float) * fluid->n * D);
+    memcpy(fluid->vel, fluid->vel_adv, sizeof(REAL) * fluid->n * D);
     gravity_acc(c, &F);
     viscosity_acc(c, &F, &F);
     surface_tension_acc(c, &F, &F);
@@ -545,7 +603,7 @@ int port_substep(void *h, tsph_set *fluid, tsph_set *bound, port_stats *out) {
     if (c->p.fbm_enabled) {
         F.general_flag = 1;
         while (F.general_flag > 0) {
-            memset(fluid->volume_frac_tmp, 0, sizeof(float) * fluid->n * P);
+            memset(fluid->volume_frac_tmp, 0, sizeof(REAL) * fluid->n * P);
             fbm_convect(c, &F, &F);
             fbm_diffuse(c, &F, &F);
             fbm_check_tmp(c, &F);
@@ -554,6 +612,8 @@ int port_substep(void *h, tsph_set *fluid, tsph_set *bound, port_stats *out) {
         }
     }
     update_tail(c, &F, c->p.fbm_enabled);
+    rset_out(c, &fr, fluid_set);
+    rset_out(c, &br, bound_set);
     if (out) {
         out->dt = c->dt;
         out->time_count = c->time_count;

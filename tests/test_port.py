@@ -34,9 +34,10 @@ def test_port_one_step(scene):
 @pytest.mark.parametrize("scene", G.SCENES)
 def test_port_fp64_one_step(scene):
     """The FP64 build of the restatement (the one-step oracle at the benchmark
-    sizes) against the numpy oracle: the two differ only in the FP32 rounding of
-    the particle arrays between kernels, so iteration counts are identical and
-    every compared field agrees within 1e-6 of its scale."""
+    sizes) against the numpy oracle: both compute and store every field in FP64
+    within a substep, so they differ by the FP32 rounding of the returned arrays
+    and by summation order: identical iteration counts, every compared field
+    within 2e-7 of its scale."""
     init, gold = G.load(scene)
     cfg = sph_config.load(*G.paths(scene))
     fa, ba = G.init_arrays(init, "fluid"), G.init_arrays(init, "bound")
@@ -55,5 +56,5 @@ def test_port_fp64_one_step(scene):
         a = getattr(sim.fluid, f).astype(np.float64)
         b = np.asarray(getattr(fl, f)).reshape(a.shape)
         scale = max(float(np.abs(b).max()), dens if f == "psi_adv" else 0.0)
-        assert np.abs(a - b).max() <= 1e-6 * max(scale, 1e-30), (scene, f, np.abs(a - b).max(), scale)
+        assert np.abs(a - b).max() <= 2e-7 * max(scale, 1e-30), (scene, f, np.abs(a - b).max(), scale)
     sim.close()
