@@ -3,7 +3,7 @@
 The golden scenes pin the CUDA path on states of ~100-200 particles a few
 substeps after rest.  These tests check the same one-step bar on the benchmark
 workloads after the flow has developed (the pressure solves iterate past their
-floor):
+floor where the workload's time step lets them):
 
 1. the CUDA path runs ``develop`` substeps of the workload from rest;
 2. its FP32 state (positions, velocities, masses, rest densities / volumes,
@@ -18,11 +18,27 @@ compared field within 1e-5 of its scale max|oracle| (``psi_adv`` is a difference
 of the solver's psi, so its scale is psi's: the density for DFSPH, the
 compression ratio for VFSPH; with the volume-fraction update ``acce_adv`` is
 (v_adv - vel) / dt and is scaled by max|v_adv| / dt); masses and rest densities
-2e-6; cell codes and solver iteration counts exactly equal; dt 1e-6 relative;
-compression 1e-3 relative; energies 1e-5.
+2e-6, except with the volume-fraction update, where they are sums of the updated
+volume fractions (rho0 = sum_k rho_k vf_k, m = rho0 V) and carry their 1e-5; cell
+codes and solver iteration counts exactly equal; dt 1e-6 relative; compression
+1e-3 relative; energies 1e-5; the volume-fraction loop's pass count equal to
+FP64's or to the reference FP32 arithmetic's (a particle whose volume fraction
+plus its increment lands at ~0 is flagged or not by rounding).
+
+One exception, stated with its cause: in the two-phase VFSPH state psi is the
+compression ratio (~1) and psi_adv = psi - 1 + ... is ~1e-6 of it, so FP32's
+~1e-7 rounding of psi (spline evaluation, reciprocal square root) is a tenth of
+psi_adv and of the pressure correction of the velocity.  No FP32 evaluation of
+the reference's algorithm meets 1e-5 on velocity there: the FP32 build of the
+restatement (the reference's own arithmetic) run from the same state misses it
+too, and the test measures that miss.  The velocities (and the velocity
+differences built on them, acce_adv and drift_vel) must then be no farther from
+the FP64 oracle than 1.5 times the reference arithmetic's own distance (or
+within 1e-5); every other field keeps the 1e-5 bar.
 
 Workloads: the 3D dam break of 1,000,000 fluid + 566,742 boundary particles
-after 250 substeps; the 3D two-phase VFSPH pair of blocks (2,000,000 fluid
+after 250 substeps, and at five times its time step after 100 substeps (where
+the density solve iterates past its floor); the 3D two-phase VFSPH pair of blocks (2,000,000 fluid
 particles, surface tension 0.07, volume-fraction update on) after 60 substeps;
 the 2D dam break of 5,000 particles after 500 and after 999 substeps (its
 stated run is 1,000 substeps).
@@ -53,10 +69,12 @@ def _err(a, b, scale):
     return float(np.abs(a.astype(np.float64) - b.astype(np.float64)).max(initial=0.0)) / max(scale, 1e-30)
 
 
-def _one_step_after(cfg_d, scen_d, develop, fbm=False, noise=None):
+def _one_step_after(cfg_d, scen_d, develop, fbm=False, noise=None, fp32_reference=False):
     """Develops the workload on the GPU, then one substep on the GPU and on the
     FP64 restatement from the same state; returns the worst relative error per
-    field and the iteration counts of the compared substep."""
+    field and the iteration counts of the compared substep.  With
+    ``fp32_reference`` the FP32 build of the restatement also steps from that
+    state and its own distance from FP64 is returned as ``info["fp32_ref"]``."""
     from oracle.port import PortSim
     from tichi_sph_gb300 import sph_config
     from tichi_sph_gb300.simulation import Simulation
@@ -119,6 +137,25 @@ def _one_step_after(cfg_d, scen_d, develop, fbm=False, noise=None):
                     "dt": (gs["dt"], ps["dt"]), "compression": (gs["compression"], ps["compression"]),
                     "ke": (gs["kinetic_energy"], ps["kinetic_energy"]),
                     "pe": (gs["potential_energy"], ps["potential_energy"]), "n": (nf, nb)}
+            if fp32_reference:
+                p32 = PortSim(cfg, fa, ba, fbm=fbm, fp64=False)
+                try:
+                    p32.set_state(time_count=st0["time_count"], compression=st0["compression"])
+                    info["fp32_ref_fbm"] = p32.substep()["fbm_passes"]
+                    ref = {}
+                    for f in ("vel", "acce_adv", "drift_vel"):
+                        if f == "drift_vel" and not fbm:
+                            continue
+                        b = getattr(port.fluid, f)
+                        scale = float(np.abs(b).max())
+                        if fbm and f == "acce_adv":
+                            scale = max(scale, vmax / ps["dt"])
+                        if f == "drift_vel":
+                            scale = max(scale, vmax)
+                        ref[f] = _err(getattr(p32.fluid, f), b, scale)
+                    info["fp32_ref"] = ref
+                finally:
+                    p32.close()
             print("one step after %d substeps (%d fluid, %d boundary): %s" % (develop, nf, nb, info))
             print("worst relative errors: %s" % {k: "%.2e" % v for k, v in sorted(worst.items())})
             return worst, info
@@ -131,23 +168,48 @@ def _one_step_after(cfg_d, scen_d, develop, fbm=False, noise=None):
 def _check(worst, info, fbm=False):
     assert info["iters"] == info["port_iters"], info
     if fbm:
-        assert info["fbm"][0] == info["fbm"][1], info
+        # a particle whose volume fraction plus its increment sits at ~0 is
+        # flagged or not by rounding, which may add a pass: the count must be
+        # FP64's or the reference's FP32 arithmetic's
+        assert info["fbm"][0] in (info["fbm"][1], info.get("fp32_ref_fbm", info["fbm"][1])), info
     assert info["dt"][0] == pytest.approx(info["dt"][1], rel=1e-6)
     assert info["compression"][0] == pytest.approx(info["compression"][1], rel=1e-3, abs=1e-7)
     assert info["ke"][0] == pytest.approx(info["ke"][1], rel=1e-5)
     assert info["pe"][0] == pytest.approx(info["pe"][1], rel=1e-5)
+    ref = info.get("fp32_ref", {})
     for k, v in worst.items():
-        tol = TOL.get(k.split(" ", 1)[1], 1e-5)
+        f = k.split(" ", 1)[1]
+        tol = 1e-5 if fbm else TOL.get(f, 1e-5)
+        if k.startswith("fluid ") and f in ("vel", "vel_adv", "acce_adv", "drift_vel") and ref:
+            tol = max(tol, 1.5 * ref["vel" if f == "vel_adv" else f])
         assert v <= tol, "%s rel err %.3g > %.3g (%s)" % (k, v, tol, info)
 
 
 def test_dambreak_3d_1m_developed_one_step():
     """3D DFSPH dam break, 1,000,000 fluid + 566,742 boundary particles (the
-    headline workload) after 250 substeps; the solves iterate past their floor."""
+    headline workload) after 250 substeps, the column compressed under its
+    weight.  At this workload's time step (2e-4 s) both solves stay at their
+    floor of two iterations (measured over 1,500 substeps from rest: the
+    compression after the density solve stays below 2e-4, under its 1e-3
+    tolerance)."""
     _need_cuda()
     from tichi_sph_gb300 import workloads
     cfg_d, scen_d = workloads.dambreak_3d(100)
     worst, info = _one_step_after(cfg_d, scen_d, 250)
+    _check(worst, info)
+    assert info["compression"][1] > 0.0, info
+
+
+def test_dambreak_3d_1m_iterating_one_step():
+    """The same 1M dam break at a five times larger time step (solver_cs 10:
+    dt 1e-3), after 100 substeps: the density solve iterates past its floor, so
+    the compared substep runs the Jacobi iterations the benchmark's own time
+    step does not reach."""
+    _need_cuda()
+    from tichi_sph_gb300 import workloads
+    cfg_d, scen_d = workloads.dambreak_3d(100)
+    cfg_d["solver_cs"] = 10
+    worst, info = _one_step_after(cfg_d, scen_d, 100)
     _check(worst, info)
     assert info["iters"][1] > int(cfg_d["solver_iter_threshold_min"]), info
 
@@ -159,7 +221,7 @@ def test_twophase_3d_2m_developed_one_step():
     _need_cuda()
     from tichi_sph_gb300 import workloads
     cfg_d, scen_d, noise = workloads.twophase_3d()
-    worst, info = _one_step_after(cfg_d, scen_d, 60, fbm=True, noise=noise)
+    worst, info = _one_step_after(cfg_d, scen_d, 60, fbm=True, noise=noise, fp32_reference=True)
     _check(worst, info, fbm=True)
 
 
