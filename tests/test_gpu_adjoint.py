@@ -106,6 +106,41 @@ def test_adjoint_matches_fp64_autograd_and_fd(gamma):
     assert abs(float((gv * d).sum()) - fd_v) <= 1e-3 * abs(fd_v)
 
 
+def test_adjoint_at_the_workload_length():
+    """The differentiable workload's rollout length: 64 substeps with a
+    checkpoint every 8 (seven segments recomputed before their reverse), on the
+    2,028-particle block; gradients within 1e-3 of FP64 autograd through the
+    oracle and of FP64 central differences."""
+    _need_cuda()
+    steps = 64
+    sim, roll, v0, target, sc, x0, p = _setup(steps=steps, K=8)
+    L, gv, gmu, xT = _cuda_grad(sim, roll, v0, target)
+    roll.close()
+    v = torch.as_tensor(v0, dtype=torch.float64).requires_grad_(True)
+    m = torch.tensor(0.01, dtype=torch.float64, requires_grad=True)
+    Lr, xr = _ref_loss(sc, x0, v, m, target, steps=steps)
+    Lr.backward()
+    assert float((xT - xr.detach()).abs().max()) < 1e-5
+    assert abs(L - float(Lr.detach())) <= 1e-4 * abs(float(Lr.detach()))
+    rel_v = float((gv - v.grad).norm() / v.grad.norm())
+    rel_mu = abs(gmu - float(m.grad)) / abs(float(m.grad))
+    assert rel_v < 1e-3, rel_v
+    assert rel_mu < 1e-3, rel_mu
+    h = 1e-6
+    d = torch.as_tensor(np.random.default_rng(12).standard_normal(tuple(v.shape)))
+    with torch.no_grad():
+        vv = torch.as_tensor(v0, dtype=torch.float64)
+        mm = torch.tensor(0.01, dtype=torch.float64)
+        lo = _ref_loss(sc, x0, vv, mm - h, target, steps)[0]
+        hi = _ref_loss(sc, x0, vv, mm + h, target, steps)[0]
+        fd_mu = float(hi - lo) / (2 * h)
+        lo = _ref_loss(sc, x0, vv - h * d, mm, target, steps)[0]
+        hi = _ref_loss(sc, x0, vv + h * d, mm, target, steps)[0]
+        fd_v = float(hi - lo) / (2 * h)
+    assert abs(gmu - fd_mu) <= 1e-3 * abs(fd_mu)
+    assert abs(float((gv * d).sum()) - fd_v) <= 1e-3 * abs(fd_v)
+
+
 def test_checkpoint_interval_does_not_change_gradients():
     _need_cuda()
     out = []

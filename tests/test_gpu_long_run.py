@@ -2,8 +2,9 @@
 reference (FP32, the reference's kernel order; oracle/sph_port.c), checked
 every 25 substeps (needs a GPU):
 
-* 2D: 5,000 fluid particles at 0.02 m, dt 1e-3, 600 substeps (0.6 s, the front
-  crossing most of the tank);
+* 2D: 5,000 fluid particles at 0.02 m, dt 1e-3 (CFL-limited later), 1,000
+  substeps -- the workload's stated run (the front crossing the tank, hitting
+  the far wall and running back up it);
 * 3D: a 0.2 m cube of 8,000 fluid particles at 0.01 m in a 0.6 x 0.4 x 0.3 m
   tank with 3 boundary layers (38,982 particles), dt 5e-4, 500 substeps
   (0.25 s, the front reaching the far wall).
@@ -12,6 +13,8 @@ Checked in both:
 
 * mass conservation: the fluid's total mass is exactly that of the initial
   state, in both runs;
+* the clock: equal (1e-6) while dt sits at part_size / cs; once the CFL limit
+  binds, dt follows each run's peak speed and the clocks agree within 2e-3;
 * mean density error: the compression after each density solve stays within
   the solver's tolerance (or the solve hit its iteration cap), and the run's
   mean compression agrees with the restatement's within 5%;
@@ -65,12 +68,22 @@ def _long_run(cfg_d, scen_d, steps, spacing):
     iter_max = int(cfg_d["solver_iter_threshold_max"])
     m0 = float(np.asarray(fa["mass"], dtype=np.float64).sum())
     comp_g, comp_p = [], []
+    clock_free = False
+    dt_cap = float(np.float32(np.float32(scen_d["sim_env"]["global_part_size"]) / np.float32(cfg_d["solver_cs"])))
     try:
         for step in range(1, steps + 1):
             solver.substep()
             gs = solver.stats()
             ps = port.substep()
-            assert gs["time_count"] == pytest.approx(ps["time_count"], rel=1e-6)
+            # dt is part_size / cs until the CFL limit binds; from then on it follows
+            # the peak speed, which the two FP32 runs' diverging splashes set
+            # differently, so the clocks agree exactly only while dt sits at its cap
+            at_cap = gs["dt"] == pytest.approx(dt_cap, rel=1e-6) and ps["dt"] == pytest.approx(dt_cap, rel=1e-6)
+            if at_cap and not clock_free:
+                assert gs["time_count"] == pytest.approx(ps["time_count"], rel=1e-6)
+            else:
+                clock_free = True
+                assert gs["time_count"] == pytest.approx(ps["time_count"], rel=2e-3)
             for st in (gs, ps):
                 assert st["compression"] <= tol or st["incom_iter"] > iter_max, (step, st)
             comp_g.append(gs["compression"])
@@ -94,7 +107,7 @@ def test_dambreak_2d_long_run_against_the_restatement():
     _need_cuda()
     from tichi_sph_gb300 import workloads
     cfg_d, scen_d = workloads.dambreak_2d()
-    _long_run(cfg_d, scen_d, 600, 0.02)
+    _long_run(cfg_d, scen_d, 1000, 0.02)
 
 
 def test_dambreak_3d_long_run_against_the_restatement():
