@@ -524,8 +524,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--hostloop", action="store_true",
-                    help="host-driven solver loops instead of the CUDA graph (kernels launched one by one, "
-                         "as profilers list them)")
+                    help="host-driven solver loops instead of the CUDA graph for the warm-up and timed substeps "
+                         "(kernels launched one by one, as profilers list them)")
     ap.add_argument("--no-profile", action="store_true", help="skip the per-phase timing (roofline)")
     ap.add_argument("--tpp", type=int, default=0, help="threads per particle (0: autotune after warm-up)")
     ap.add_argument("--workload", default="dambreak3d",
@@ -570,8 +570,6 @@ def main():
         return 0
     cfg, sim = build_sim(args.n_side, dev, args.spacing)
     solver = sim.solver
-    if args.hostloop:
-        solver.set_graph_mode(False)
     nf, nb = sim.fluid.part_num[None], sim.bound.part_num[None]
     stream = torch.cuda.current_stream(dev)
 
@@ -581,6 +579,10 @@ def main():
     develop = args.develop if args.develop >= 0 else max(0, args.run_length - args.warmup - args.steps)
     for _ in range(develop):
         solver.substep()
+    if args.hostloop:
+        # the warm-up and timed substeps launch every kernel on its own (the
+        # development above runs as graphs)
+        solver.set_graph_mode(False)
     for i in range(args.warmup):
         solver.substep()
         if i == 0 and not args.tpp:
