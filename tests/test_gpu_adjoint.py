@@ -106,28 +106,62 @@ def test_adjoint_matches_fp64_autograd_and_fd(gamma):
     assert abs(float((gv * d).sum()) - fd_v) <= 1e-3 * abs(fd_v)
 
 
+def _ref_grads(sc, x0, v0, target, steps, dtype):
+    """Gradients of the oracle's loss in `dtype` (FP64: the reference; FP32: the
+    same algorithm at the forward's precision, to measure its own distance)."""
+    import copy
+    from oracle import sph_autodiff as A
+    keep = A.T
+    A.T = dtype
+    sc = copy.copy(sc)
+    for k, val in vars(sc).items():   # the scene's tensors in `dtype` too (no promotion back to FP64)
+        if torch.is_tensor(val) and val.is_floating_point():
+            setattr(sc, k, val.to(dtype))
+    try:
+        v = torch.as_tensor(v0, dtype=dtype).requires_grad_(True)
+        m = torch.tensor(0.01, dtype=dtype, requires_grad=True)
+        x, comp = x0.to(dtype), 0.0
+        w = v
+        for _ in range(steps):
+            x, w, comp, _ = A.substep(sc, x, w, m, comp, iters=(2, 2))
+        L = A.loss_fn(sc, x, torch.as_tensor(target, dtype=dtype))
+        L.backward()
+        return float(L.detach()), v.grad.double(), float(m.grad), x.detach().double()
+    finally:
+        A.T = keep
+
+
 def test_adjoint_at_the_workload_length():
     """The differentiable workload's rollout length: 64 substeps with a
     checkpoint every 8 (seven segments recomputed before their reverse), on the
-    2,028-particle block; gradients within 1e-3 of FP64 autograd through the
-    oracle and of FP64 central differences."""
+    2,028-particle block, against FP64 autograd through the oracle and FP64
+    central differences.
+
+    Over 64 substeps the active set of psi_adv = max(s, 0) drifts with the
+    forward's rounding, so no FP32 evaluation of the step reaches 1e-3 here: the
+    oracle's own autograd run in FP32 differs from its FP64 gradient by ~1.7%
+    (dL/dv0) and ~0.5% (dL/dmu), against 2e-4 and 1e-5 at 16 substeps.  The test
+    measures that distance and holds the CUDA gradients to 1.5 times it (or to
+    1e-3, whichever is larger)."""
     _need_cuda()
     steps = 64
     sim, roll, v0, target, sc, x0, p = _setup(steps=steps, K=8)
     L, gv, gmu, xT = _cuda_grad(sim, roll, v0, target)
     roll.close()
-    v = torch.as_tensor(v0, dtype=torch.float64).requires_grad_(True)
-    m = torch.tensor(0.01, dtype=torch.float64, requires_grad=True)
-    Lr, xr = _ref_loss(sc, x0, v, m, target, steps=steps)
-    Lr.backward()
-    assert float((xT - xr.detach()).abs().max()) < 1e-5
-    assert abs(L - float(Lr.detach())) <= 1e-4 * abs(float(Lr.detach()))
-    rel_v = float((gv - v.grad).norm() / v.grad.norm())
-    rel_mu = abs(gmu - float(m.grad)) / abs(float(m.grad))
-    assert rel_v < 1e-3, rel_v
-    assert rel_mu < 1e-3, rel_mu
+    Lr, g64, m64, x64 = _ref_grads(sc, x0, v0, target, steps, torch.float64)
+    _, g32, m32, _ = _ref_grads(sc, x0, v0, target, steps, torch.float32)
+    floor_v = float((g32 - g64).norm() / g64.norm())
+    floor_mu = abs(m32 - m64) / abs(m64)
+    assert float((xT - x64).abs().max()) < 5e-5   # FP32 forwards drift ~1e-5 m over 64 substeps
+    assert abs(L - Lr) <= 1e-4 * abs(Lr)
+    rel_v = float((gv - g64).norm() / g64.norm())
+    rel_mu = abs(gmu - m64) / abs(m64)
+    print("64 substeps: dL/dv0 %.3g (FP32 oracle %.3g), dL/dmu %.3g (FP32 oracle %.3g)" % (rel_v, floor_v, rel_mu,
+                                                                                           floor_mu))
+    assert rel_v < max(1e-3, 1.5 * floor_v), (rel_v, floor_v)
+    assert rel_mu < max(1e-3, 1.5 * floor_mu), (rel_mu, floor_mu)
     h = 1e-6
-    d = torch.as_tensor(np.random.default_rng(12).standard_normal(tuple(v.shape)))
+    d = torch.as_tensor(np.random.default_rng(12).standard_normal(tuple(g64.shape)))
     with torch.no_grad():
         vv = torch.as_tensor(v0, dtype=torch.float64)
         mm = torch.tensor(0.01, dtype=torch.float64)
@@ -137,8 +171,8 @@ def test_adjoint_at_the_workload_length():
         lo = _ref_loss(sc, x0, vv - h * d, mm, target, steps)[0]
         hi = _ref_loss(sc, x0, vv + h * d, mm, target, steps)[0]
         fd_v = float(hi - lo) / (2 * h)
-    assert abs(gmu - fd_mu) <= 1e-3 * abs(fd_mu)
-    assert abs(float((gv * d).sum()) - fd_v) <= 1e-3 * abs(fd_v)
+    assert abs(gmu - fd_mu) <= max(1e-3, 1.5 * floor_mu) * abs(fd_mu)
+    assert abs(float((gv * d).sum()) - fd_v) <= max(1e-3, 1.5 * floor_v) * abs(fd_v)
 
 
 def test_checkpoint_interval_does_not_change_gradients():

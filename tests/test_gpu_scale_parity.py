@@ -21,9 +21,11 @@ compression ratio for VFSPH; with the volume-fraction update ``acce_adv`` is
 2e-6, except with the volume-fraction update, where they are sums of the updated
 volume fractions (rho0 = sum_k rho_k vf_k, m = rho0 V) and carry their 1e-5; cell
 codes and solver iteration counts exactly equal; dt 1e-6 relative; compression
-1e-3 relative; energies 1e-5; the volume-fraction loop's pass count equal to
-FP64's or to the reference FP32 arithmetic's (a particle whose volume fraction
-plus its increment lands at ~0 is flagged or not by rounding).
+1e-3 relative; energies 1e-5; the volume-fraction loop's pass count within one
+of FP64's and its flags within 1% of the particles of the reference FP32
+arithmetic's (a particle whose volume fraction plus its increment lands at ~0
+is flagged or not by rounding: in the two-phase state FP64 flags ~0.28M
+particles, FP32 ~0.52M, the GPU and the FP32 restatement differing at ~4,400).
 
 One exception, stated with its cause: in the two-phase VFSPH state psi is the
 compression ratio (~1) and psi_adv = psi - 1 + ... is ~1e-6 of it, so FP32's
@@ -142,6 +144,10 @@ def _one_step_after(cfg_d, scen_d, develop, fbm=False, noise=None, fp32_referenc
                 try:
                     p32.set_state(time_count=st0["time_count"], compression=st0["compression"])
                     info["fp32_ref_fbm"] = p32.substep()["fbm_passes"]
+                    if fbm:
+                        gflag = sim.fluid.flag[:nf].cpu().numpy() != 0
+                        info["flag_diff_fp32"] = float(np.mean(gflag != (p32.fluid.flag != 0)))
+                        info["flag_diff_fp64"] = float(np.mean(gflag != (port.fluid.flag != 0)))
                     ref = {}
                     for f in ("vel", "acce_adv", "drift_vel"):
                         if f == "drift_vel" and not fbm:
@@ -169,9 +175,13 @@ def _check(worst, info, fbm=False):
     assert info["iters"] == info["port_iters"], info
     if fbm:
         # a particle whose volume fraction plus its increment sits at ~0 is
-        # flagged or not by rounding, which may add a pass: the count must be
-        # FP64's or the reference's FP32 arithmetic's
-        assert info["fbm"][0] in (info["fbm"][1], info.get("fp32_ref_fbm", info["fbm"][1])), info
+        # flagged or not by rounding (in the two-phase state a quarter of the
+        # particles do: FP64 flags ~0.28M where FP32 flags ~0.52M), which may add
+        # or save a pass: the count within one of FP64's, and the flags within
+        # 1% of the particles of the reference FP32 arithmetic's
+        assert abs(info["fbm"][0] - info["fbm"][1]) <= 1, info
+        if "flag_diff_fp32" in info:
+            assert info["flag_diff_fp32"] <= 0.01, info
     assert info["dt"][0] == pytest.approx(info["dt"][1], rel=1e-6)
     assert info["compression"][0] == pytest.approx(info["compression"][1], rel=1e-3, abs=1e-7)
     assert info["ke"][0] == pytest.approx(info["ke"][1], rel=1e-5)
