@@ -540,6 +540,24 @@ struct Lanes {
     }
 };
 
+// List loads that do not allocate in L1: each entry of the neighbour list is
+// read once per sweep, while the neighbours' fields it points to are read by
+// many particles of a block; left to allocate, the list (~37 KB per block)
+// evicts them.  The .nc form is for lists written by an earlier launch; the
+// other orders after the calling thread's own stores of the list.
+__device__ __forceinline__ int4 ld_list_nc(const int4 *p) {
+    int4 r;
+    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ int4 ld_list(const int4 *p) {
+    int4 r;
+    asm volatile("ld.global.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p) : "memory");
+    return r;
+}
+
 // Walks the blocked neighbour list of sorted particle s for lane q of a TPP-lane
 // group: blocks b = q, q + TPP, ... of four entries; entries t < nfl are fluid
 // neighbours (ff), nfl <= t < ntot boundary ones (fb).  The next block's int4 is
@@ -554,7 +572,7 @@ __device__ __forceinline__ void walk_blocks(const int *__restrict__ nbr, int64_t
     const int nblk = (ntot + 3) >> 2;
     int b = q;
     if (b >= nblk) return;
-    auto ld = [&](int64_t i) { return NC ? __ldg(L4 + i) : L4[i]; };
+    auto ld = [&](int64_t i) { return NC ? ld_list_nc(L4 + i) : ld_list(L4 + i); };
     int4 cur = ld((int64_t)b * cap);
     while (b < nblk) {
         const int bn = b + TPP;
@@ -586,11 +604,11 @@ __device__ __forceinline__ void walk_range_pred(const int4 *__restrict__ L4, int
     const int b0 = lo >> 2, b1 = (hi + 3) >> 2;
     int b = b0 + ((q - b0) & (TPP - 1));
     if (b >= b1) return;
-    int4 cur = __ldg(L4 + (int64_t)b * cap);
+    int4 cur = ld_list_nc(L4 + (int64_t)b * cap);
     while (b < b1) {
         const int bn = b + TPP;
         int4 nxt = cur;
-        if (bn < b1) nxt = __ldg(L4 + (int64_t)bn * cap);
+        if (bn < b1) nxt = ld_list_nc(L4 + (int64_t)bn * cap);
         const int t0 = b << 2;
         const int first = lo > t0 ? lo - t0 : 0;  // first in-range entry (0..3)
         const int jf = first == 0 ? cur.x : first == 1 ? cur.y : first == 2 ? cur.z : cur.w;
