@@ -167,6 +167,10 @@ struct Geo {
 // nbr_cnt value of a particle whose neighbours did not fit the list: its sweeps
 // scan the template cells instead.
 constexpr unsigned int kNbrOverflow = 0xffffffffu;
+// normal.w of a particle without surface tension: a NaN bit pattern that no
+// arithmetic produces (the hardware's NaN results are 0x7fffffff)
+constexpr unsigned int kNoSurfTension = 0xffffffffu;
+__device__ __forceinline__ bool has_surf_tension(float4 n) { return __float_as_uint(n.w) != kNoSurfTension; }
 
 // Position of neighbour t of sorted particle s in the blocked neighbour list.
 __host__ __device__ __forceinline__ int64_t nbr_index(int t, int64_t s, int64_t cap) {
@@ -187,6 +191,8 @@ struct FluidBuf {
     float *psiadv, *kappa;   // psi_adv and psi_adv / alpha
     float4 *pk;              // (x, y, z, kappa): what the velocity sweep reads of a neighbour
     float4 *acc;       // acce_adv
+    // surface normal (x, y, z); w = the particle's psi when its phase-0 volume
+    // fraction exceeds 0.99 (it takes part in surface tension), else kNoSurfTension
     float4 *normal;
     float4 *dens;      // W, sph_density, sph_compression, alpha_2: read together by the write-back
     float4 *a1;

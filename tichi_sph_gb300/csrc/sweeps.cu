@@ -666,16 +666,23 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
     nx = ln.sum(nx);
     ny = ln.sum(ny);
     nz = ln.sum(nz);
-    if (act && ln.q == 0) F.normal[s] = make_float4(nx * g.h, ny * g.h, nz * g.h, 0.f);
+    if (act && ln.q == 0) {
+        // w: what the surface-tension pass reads of a neighbour beside its normal
+        const float w = F.vf[s] > 0.99f ? F.mpsi[s].y : __uint_as_float(kNoSurfTension);
+        F.normal[s] = make_float4(nx * g.h, ny * g.h, nz * g.h, w);
+    }
 }
 
 // SPH_vel_adv_2_vel + SPH_advection_gravity_acc + SPH_advection_viscosity_acc
 // + (pass 2 of) SPH_advection_surface_tension_acc + SPH_advection_update_vel_adv,
 // sph.py:108-166, 247-262.  The curvature term of the surface tension has no
 // kernel weight, so -- like the reference -- it runs over every candidate in the
-// template cells, not only those within h: with surface tension on this sweep
-// scans the cells; without it, it walks the neighbour list.  gs / vs scale the
-// gravity / viscosity terms by 1 or 0 (kernel-level calls may leave either
+// template cells, not only those within h: a warp holding a particle with
+// surface tension (phase-0 volume fraction above 0.99) scans the cells; any
+// other warp walks the neighbour list for the viscosity alone.  A scanned
+// candidate beyond h adds only the curvature term (the cohesion kernel is zero
+// there), read from the neighbour's normal and psi in one load.  gs / vs scale
+// the gravity / viscosity terms by 1 or 0 (kernel-level calls may leave either
 // out; x * 1 is exact, so the full step's bits are unchanged).
 template <int DIM, bool ST, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBuf B, float gs, float vs) {
@@ -693,13 +700,18 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
     float vx = 0.f, vy = 0.f, vz = 0.f;   // viscosity sum
     float sx = 0.f, sy = 0.f, sz = 0.f;   // surface tension sum
     float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool st_i = false;
+    if (ST && act) {
+        ni = F.normal[s];
+        st_i = has_surf_tension(ni);
+    }
+    // every lane of the warp reaches this vote (no lane has returned)
+    const bool scan = ST && __any_sync(0xffffffffu, st_i);
     if (act) {
         const float4 pi = F.pos[s];
         vi = vin[s];
         const float4 mpi = F.mpsi[s];
-        const float vfi0 = ST ? F.vf[s] : 0.f;
-        const float4 ni = ST ? F.normal[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const bool st_i = ST && vfi0 > 0.99f;
         const float lap = 2.f * (2.f + DIM);
         const float eps = 0.01f * g.h2;
         const float gamma = c.gamma, c_coh = c.c_coh;
@@ -708,33 +720,32 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (!(r2 > 0.f)) return;
-            if (r2 < g.h2) {
+            const bool near = r2 < g.h2;
+            float r = 0.f, ri = 0.f, mj = 0.f;
+            if (near) {
                 const float4 vj = vin[j];
-                const float psij = F.mpsi[j].y;
-                float r;
-                const float ri = pair_rinv(r2, r);
+                const float4 mpj = F.mpsi[j];
+                mj = mpj.x;
+                ri = pair_rinv(r2, r);
                 const float wg = kwg(r * g.inv_h) * g.sig_h;
                 const float adx = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-                const float f = __fdividef(lap * __fdividef(pj.w, psij) * wg * ri * adx, eps + r2);
+                const float f = __fdividef(lap * __fdividef(pj.w, mpj.y) * wg * ri * adx, eps + r2);
                 vx += f * dx;
                 vy += f * dy;
                 vz += f * dz;
             }
             if (ST && st_i) {
-                if (F.vf[j] > 0.99f) {
-                    const float4 mpj = F.mpsi[j];
-                    const float4 nj = F.normal[j];
-                    float r;
-                    const float ri = pair_rinv(r2, r);
-                    const float coh = -gamma * mpj.x * (kcoh(r * g.inv_h) * c_coh) * ri;
-                    const float fac = __fdividef(2.f * mpi.z, mpi.y + mpj.y);
+                const float4 nj = F.normal[j];   // w: the neighbour's psi
+                if (has_surf_tension(nj)) {
+                    const float coh = near ? -gamma * mj * (kcoh(r * g.inv_h) * c_coh) * ri : 0.f;
+                    const float fac = __fdividef(2.f * mpi.z, mpi.y + nj.w);
                     sx += fac * (coh * dx + gamma * (ni.x - nj.x));
                     sy += fac * (coh * dy + gamma * (ni.y - nj.y));
                     sz += fac * (coh * dz + gamma * (ni.z - nj.z));
                 }
             }
         };
-        if (ST) {
+        if (scan) {
             bool ok;
             const long long code = cell_code<DIM>(pi, g, ok);
             if (ok) visit_candidates<DIM, TPP>(F.start, g, code, shift_of<M>(st.f_shift), ln.q, pair);
