@@ -11,7 +11,9 @@
  * baseline) or double (the FP64 oracle: every field, sum and pair term in
  * double; the FP32 particle arrays are converted to double working arrays at
  * the start of a substep and back at its end).  OpenMP parallelises the
- * outermost particle loop of every kernel, as Taichi's CPU backend does.
+ * outermost particle loop of every kernel, as Taichi's CPU backend does, but
+ * for the cell fill and the solvers' compression sum, which run serially so
+ * that every run of the restatement gives the same bits.
  */
 #include <math.h>
 #include <stdint.h>
@@ -128,15 +130,16 @@ static void mem_shift(port_ctx *c) {
     }
 }
 
+/* The reference fills a cell through an atomic counter (any order of its
+ * particles is valid); this fill runs serially, so each cell holds its
+ * particles in id order on every run, as the CUDA path's cells do: the
+ * restatement's sums then run in one fixed order. */
 static void fill_node(port_ctx *c, obj_t *o) {
     rset *s = o->s;
-#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < s->n; ++i) {
         int32_t code = s->neighb_cell_seq[i];
         if (0 < code && code < c->p.node_num) {
-            int32_t slot;
-#pragma omp atomic capture
-            slot = c->node_part_shift_count[code]++;
+            int32_t slot = c->node_part_shift_count[code]++;
             s->neighb_in_cell_seq[i] = slot;
             c->part_pid_in_node[slot] = (int32_t)i;
             c->part_uid_in_node[slot] = o->uid;
@@ -334,13 +337,14 @@ static void adv_psi(port_ctx *c, obj_t *o, obj_t *no) {
     }
 }
 
+/* The sum runs serially in id order: an OpenMP reduction combines the threads'
+ * partial sums in no fixed order, and the solver loops branch on this value. */
 static void psi_adv_non_negative(port_ctx *c, obj_t *o) {
-    REAL sum = 0;
-#pragma omp parallel for schedule(static) reduction(+ : sum)
-    for (int64_t i = 0; i < o->s->n; ++i) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < o->s->n; ++i)
         if (o->s->psi_adv[i] < 0) o->s->psi_adv[i] = 0;
-        sum += o->s->psi_adv[i] / rest_psi(o, i);
-    }
+    REAL sum = 0;
+    for (int64_t i = 0; i < o->s->n; ++i) sum += o->s->psi_adv[i] / rest_psi(o, i);
     c->compression = sum / (REAL)o->s->n;
 }
 
