@@ -76,7 +76,9 @@ __global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F) {
             dx *= 0.f; dy *= 0.f; dz *= 0.f;
         }
         dx += fx - ax; dy += fy - ay; dz += fz - az;
-        F.drift[q * F.cap + s] = make_float4(dx * dt, dy * dt, dz * dt, 0.f);
+        // w: the phase's volume fraction, which no pass changes (the passes
+        // read a neighbour's drift and volume fraction in one load)
+        F.drift[q * F.cap + s] = make_float4(dx * dt, dy * dt, dz * dt, vf[q]);
     }
     F.acc[s] = make_float4(ax, ay, az, 0.f);
     F.facc[s] = make_float4(fx, fy, fz, 0.f);
@@ -129,13 +131,13 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, Bound
                     float r;
                     const float ri = pair_rinv_pos(r2, r);
                     const float wg = kwg(r * g.inv_h) * g.sig_h;
-                    const float Vj = F.mv[j].y;
+                    const float Vj = k.vfsph ? pj.w : F.mv[j].y;  // VFSPH: X = rest volume
                     const float gx = dx * ri * wg, gy = dy * ri * wg, gz = dz * ri * wg;
                     const float dif = __fdividef(cd * Vj * r * wg, r2 + eps);
 #pragma unroll
                     for (int q = 0; q < P; ++q) {
-                        const float vfj = F.vf[q * F.cap + j];
                         const float4 uj = F.drift[q * F.cap + j];
+                        const float vfj = uj.w;
                         const float fx = vfi[q] * ui[q].x + vfj * uj.x;
                         const float fy = vfi[q] * ui[q].y + vfj * uj.y;
                         const float fz = vfi[q] * ui[q].z + vfj * uj.z;
