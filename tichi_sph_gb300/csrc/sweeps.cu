@@ -218,7 +218,9 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
         if (ok) {
             // phase 1: record the pairs.  The write position walks the blocked
             // layout (entry t at nbr_index(t, s, stride)): +1 within a block of
-            // four, +4 stride - 3 to the next block
+            // four, +4 stride - 3 to the next block.  Candidate positions load
+            // through the read-only path (no step writes them in this kernel),
+            // so they need not wait for the list stores before them
             int nrec = 0;
             int *wp = L + (int64_t)s * 4;
             const int64_t next_block = stride * 4 - 3;
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
                 ++nrec;
             };
             visit_candidates_within<DIM>(F.start, g, pi, code, f_shift, 0, [&](int j) {
-                const float4 pj = F.pos[j];
+                const float4 pj = __ldg(&F.pos[j]);
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < g.h2) {
@@ -246,7 +248,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
             });
             nfl = nrec;
             visit_candidates_within<DIM>(B.start, g, pi, code, b_shift, 0, [&](int j) {
-                const float4 pj = B.pos[j];
+                const float4 pj = __ldg(&B.pos[j]);
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < g.h2) {
@@ -675,14 +677,18 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
 
 // SPH_vel_adv_2_vel + SPH_advection_gravity_acc + SPH_advection_viscosity_acc
 // + (pass 2 of) SPH_advection_surface_tension_acc + SPH_advection_update_vel_adv,
-// sph.py:108-166, 247-262.  The curvature term of the surface tension has no
-// kernel weight, so -- like the reference -- it runs over every candidate in the
-// template cells, not only those within h: a warp holding a particle with
-// surface tension (phase-0 volume fraction above 0.99) scans the cells; any
-// other warp walks the neighbour list for the viscosity alone.  A scanned
-// candidate beyond h adds only the curvature term (the cohesion kernel is zero
-// there), read from the neighbour's normal and psi in one load.  gs / vs scale
-// the gravity / viscosity terms by 1 or 0 (kernel-level calls may leave either
+// sph.py:108-166, 247-262.  The list gives the pairs within h: viscosity and,
+// for a particle with surface tension (phase-0 volume fraction above 0.99), the
+// cohesion term of every such neighbour (zero beyond h).  The curvature term
+// has no kernel weight, so -- like the reference -- it runs over every
+// candidate of the template cells, not only those within h: a second loop over
+// the cells that reads each candidate's normal and psi in one load.  Its only
+// distance test, r > 0, needs no position: the terms it would drop are exactly
+// zero, the particle's own (n_i - n_i) and that of a particle at its exact
+// position (the two have the same neighbours in the same order, each leaving
+// the other out, so the same normal bit for bit).  A particle whose list overflowed takes the
+// reference's form with the range tests per candidate.  gs / vs scale the
+// gravity / viscosity terms by 1 or 0 (kernel-level calls may leave either
 // out; x * 1 is exact, so the full step's bits are unchanged).
 template <int DIM, bool ST, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBuf B, float gs, float vs) {
@@ -700,21 +706,17 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
     float vx = 0.f, vy = 0.f, vz = 0.f;   // viscosity sum
     float sx = 0.f, sy = 0.f, sz = 0.f;   // surface tension sum
     float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool st_i = false;
-    if (ST && act) {
-        ni = F.normal[s];
-        st_i = has_surf_tension(ni);
-    }
-    // every lane of the warp reaches this vote (no lane has returned)
-    const bool scan = ST && __any_sync(0xffffffffu, st_i);
     if (act) {
         const float4 pi = F.pos[s];
         vi = vin[s];
         const float4 mpi = F.mpsi[s];
+        const float4 ni = ST ? F.normal[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool st_i = ST && has_surf_tension(ni);
         const float lap = 2.f * (2.f + DIM);
         const float eps = 0.01f * g.h2;
         const float gamma = c.gamma, c_coh = c.c_coh;
+        const long long f_shift = shift_of<M>(st.f_shift);
+        // every term of one candidate, with the reference's range tests
         auto pair = [&](int j) {
             const float4 pj = F.pos[j];
             const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -745,18 +747,20 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                 }
             }
         };
-        if (scan) {
-            bool ok;
-            const long long code = cell_code<DIM>(pi, g, ok);
-            if (ok) visit_candidates<DIM, TPP>(F.start, g, code, shift_of<M>(st.f_shift), ln.q, pair);
+        const bool exact = ST && st_i && F.nbr_cnt[s] == kNbrOverflow;
+        bool ok = false;
+        long long code = 0;
+        if (ST && st_i) code = cell_code<DIM>(pi, g, ok);
+        if (exact) {
+            if (ok) visit_candidates<DIM, TPP>(F.start, g, code, f_shift, ln.q, pair);
         } else {
-            // viscosity only: list entries skip the range tests and load their
-            // neighbour's v_adv and psi together with its position
+            // list entries skip the range tests and load their neighbour's v_adv
+            // and psi together with its position
             for_each_neighbor_tpp<DIM, false, TPP, M>(c, st, k.R, F, B, s, ln.q, pi,
                 [&](int j, auto listed) {
                     constexpr bool L = decltype(listed)::value;
                     if (!L) {
-                        pair(j);
+                        pair(j);  // (a particle with surface tension is not here)
                         return;
                     }
                     const float4 pj = F.pos[j];
@@ -774,8 +778,31 @@ __global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBu
                     vx += f * dx;
                     vy += f * dy;
                     vz += f * dz;
+                    if (ST && st_i) {
+                        const float4 nj = F.normal[j];
+                        if (has_surf_tension(nj)) {
+                            const float mj = F.mv[j].x;
+                            const float coh = -gamma * mj * (kcoh(r * g.inv_h) * c_coh) * ri;
+                            const float fac = __fdividef(2.f * mpi.z, mpi.y + nj.w);
+                            sx += fac * (coh * dx);
+                            sy += fac * (coh * dy);
+                            sz += fac * (coh * dz);
+                        }
+                    }
                 },
                 [&](int, auto) {});
+            if (ST && st_i && ok) {
+                // the curvature term over every candidate of the template cells
+                visit_candidates<DIM, TPP>(F.start, g, code, f_shift, ln.q, [&](int j) {
+                    const float4 nj = F.normal[j];
+                    if (has_surf_tension(nj)) {
+                        const float fac = __fdividef(2.f * mpi.z, mpi.y + nj.w);
+                        sx += fac * (gamma * (ni.x - nj.x));
+                        sy += fac * (gamma * (ni.y - nj.y));
+                        sz += fac * (gamma * (ni.z - nj.z));
+                    }
+                });
+            }
         }
     }
     vx = ln.sum(vx);
