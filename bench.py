@@ -328,15 +328,17 @@ def batched_line(res, args, ws):
                        "mean_div_iter": res["mean_div_iter"], "mean_incom_iter": res["mean_incom_iter"]}}
 
 
-def run_other(kind, steps, warmup, dev, develop=0):
-    """The two-phase VFSPH block pair or the 2D dam break through the plain path:
-    ``develop`` untimed substeps from rest, ``warmup`` more, then ``steps`` timed."""
+def run_other(kind, steps, warmup, dev, develop=0, n_side=100, hostloop=False):
+    """The two-phase VFSPH block pair (two cubes of ``n_side``^3 particles) or the
+    2D dam break through the plain path: ``develop`` untimed substeps from rest,
+    ``warmup`` more, then ``steps`` timed; ``hostloop``: the warm-up and timed
+    substeps launch every kernel on its own."""
     import numpy as np
     import torch
     from tichi_sph_gb300 import sph_config, workloads
     from tichi_sph_gb300.simulation import Simulation
     if kind == "twophase3d":
-        c, sc, noise = workloads.twophase_3d()
+        c, sc, noise = workloads.twophase_3d(n_side=n_side)
         fbm = True
     else:
         c, sc = workloads.dambreak_2d()
@@ -351,7 +353,11 @@ def run_other(kind, steps, warmup, dev, develop=0):
         sim.fluid.update_mass_all()
     s = sim.solver
     stream = torch.cuda.current_stream(dev)
-    for _ in range(develop + warmup):
+    for _ in range(develop):
+        s.substep()
+    if hostloop:
+        s.set_graph_mode(False)
+    for _ in range(warmup):
         s.substep()
     torch.cuda.synchronize(dev)
     s0 = s.stats()
@@ -375,8 +381,10 @@ def run_other(kind, steps, warmup, dev, develop=0):
 
 
 def other_line(res, args, ws):
-    desc = {"twophase3d": "3D two-phase VFSPH, two 1 m cubes (rest density 1000 / 500) of 1M particles each, "
-                          "spacing 0.01, surface tension 0.07, volume-fraction update on",
+    n3 = res["fluid_particles"] // 2
+    side = "%.2f m cubes" % (round(n3 ** (1 / 3)) * 0.01)
+    desc = {"twophase3d": "3D two-phase VFSPH, two %s (rest density 1000 / 500) of %d particles each, "
+                          "spacing 0.01, surface tension 0.07, volume-fraction update on" % (side, n3),
             "dambreak2d": "2D DFSPH dam break, 1.0 x 2.0 m block at 0.02 m (5,000 particles), 4 x 4 m box, "
                           "dt 1e-3"}[res["kind"]]
     return {"metric": METRIC, "value": res["fluid_particles"] * ws / (res["ms"] / 1e3), "unit": UNIT, "n_gpus": ws,
@@ -562,7 +570,8 @@ def main():
             dist.destroy_process_group()
         return 0
     if args.workload in ("twophase3d", "dambreak2d"):
-        res = run_other(args.workload, args.steps, args.warmup, dev)
+        res = run_other(args.workload, args.steps, args.warmup, dev, develop=max(args.develop, 0),
+                        n_side=args.n_side, hostloop=args.hostloop)
         if rank == 0:
             print(json.dumps(other_line(res, args, ws)), flush=True)
         if dist:

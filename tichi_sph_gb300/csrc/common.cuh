@@ -197,7 +197,7 @@ struct FluidBuf {
     float4 *dens;      // W, sph_density, sph_compression, alpha_2: read together by the write-back
     float4 *a1;
     float *vf, *vftmp;       // [P][cap]
-    float4 *drift;           // [P][cap]
+    float4 *drift;           // [cap][P]: a particle's phases side by side (the pass gathers them together)
     float4 *facc;            // acce (fbm_acce)
     float *zeta;
     int *flagpass;           // 0 = unflagged, else the FBM pass that flagged it

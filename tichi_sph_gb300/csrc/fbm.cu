@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F) {
         dx += fx - ax; dy += fy - ay; dz += fz - az;
         // w: the phase's volume fraction, which no pass changes (the passes
         // read a neighbour's drift and volume fraction in one load)
-        F.drift[q * F.cap + s] = make_float4(dx * dt, dy * dt, dz * dt, vf[q]);
+        F.drift[s * P + q] = make_float4(dx * dt, dy * dt, dz * dt, vf[q]);
     }
     F.acc[s] = make_float4(ax, ay, az, 0.f);
     F.facc[s] = make_float4(fx, fy, fz, 0.f);
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, Bound
             const float4 pi = F.pos[s];
             float4 ui[P];
 #pragma unroll
-            for (int q = 0; q < P; ++q) ui[q] = F.drift[q * F.cap + s];
+            for (int q = 0; q < P; ++q) ui[q] = F.drift[s * P + q];
             const float cc = c.fbm_c * dt, cd = dt * c.fbm_D, eps = 0.01f * g.h2;
             for_each_neighbor_tpp<DIM, false, 1, true>(c, st, k.R, F, B, s, 0, pi,
                 [&](int j, auto) {
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, Bound
                     const float dif = __fdividef(cd * Vj * r * wg, r2 + eps);
 #pragma unroll
                     for (int q = 0; q < P; ++q) {
-                        const float4 uj = F.drift[q * F.cap + j];
+                        const float4 uj = F.drift[(int64_t)j * P + q];
                         const float vfj = uj.w;
                         const float fx = vfi[q] * ui[q].x + vfj * uj.x;
                         const float fy = vfi[q] * ui[q].y + vfj * uj.y;

@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
 #pragma unroll
             for (int d = 0; d < DIM; ++d) U.acce[b + d] = fav[d];
             for (int q = 0; q < k.P; ++q) {
-                const float4 dv = F.drift[q * F.cap + s];
+                const float4 dv = F.drift[s * k.P + q];
                 const float dvv[3] = {dv.x, dv.y, dv.z};
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) U.drift_vel[(pid * k.P + q) * DIM + d] = dvv[d];
