@@ -12,16 +12,21 @@ the whole scene; the metric counts fluid particles only (particle-steps/s =
 fluid particles x substeps / time; boundary particles are not counted).  The
 timed window is the end of the 500-substep run: the flow first develops for
 500 - W - K untimed substeps (``--develop``), then W warm-up and K timed
-substeps follow, so the pressure solves iterate as they do once the column has
-loaded the floor, not at their floor of two iterations as right after rest.
+substeps follow: the developed flow (the column collapsed and running along
+the floor), not the lattice right after rest.  At this time step the pressure
+solves still converge at their floor of two iterations each; the extra entry
+``dambreak3d_cs10`` times the same scene at a five times larger step, where
+they iterate.
 
 The same line carries the other workloads of the hot path, each timed with CUDA
 events at N = 1: ``batched`` (256 dam breaks of uneven size in one launch
 against the same scenes stepped one at a time), ``twophase3d`` (2M-particle
 two-phase VFSPH with surface tension and the volume-fraction update, the end of
 its 300-substep run), ``dambreak2d`` (5,000-particle 2D dam break, substeps 4 to
-1,000 of its run) and ``adjoint`` (backward / forward time of the differentiable
-64-substep rollout of a 99,452-particle block).
+1,000 of its run), ``dambreak3d_cs10`` (the headline scene at solver_cs 10, the
+last 20 of 100 substeps: 0.1 s of flow as in the headline's 500) and ``adjoint``
+(backward / forward time of the differentiable 64-substep rollout of a
+99,452-particle block).
 
 Output: one JSON line on rank 0.  ``value`` is timed with CUDA events on the
 solver's stream around K substeps whose inputs are already on the GPU; ``e2e``
@@ -329,10 +334,12 @@ def batched_line(res, args, ws):
 
 
 def run_other(kind, steps, warmup, dev, develop=0, n_side=100, hostloop=False):
-    """The two-phase VFSPH block pair (two cubes of ``n_side``^3 particles) or the
-    2D dam break through the plain path: ``develop`` untimed substeps from rest,
-    ``warmup`` more, then ``steps`` timed; ``hostloop``: the warm-up and timed
-    substeps launch every kernel on its own."""
+    """The two-phase VFSPH block pair (two cubes of ``n_side``^3 particles), the
+    2D dam break, or (``dambreak3d_cs10``) the headline dam break at a five times
+    larger time step (solver_cs 10, dt up to 1e-3), where the Jacobi solves
+    iterate past their floor, through the plain path: ``develop`` untimed
+    substeps from rest, ``warmup`` more, then ``steps`` timed; ``hostloop``: the
+    warm-up and timed substeps launch every kernel on its own."""
     import numpy as np
     import torch
     from tichi_sph_gb300 import sph_config, workloads
@@ -340,6 +347,10 @@ def run_other(kind, steps, warmup, dev, develop=0, n_side=100, hostloop=False):
     if kind == "twophase3d":
         c, sc, noise = workloads.twophase_3d(n_side=n_side)
         fbm = True
+    elif kind == "dambreak3d_cs10":
+        c, sc = workloads.dambreak_3d(n_side)
+        c["solver_cs"] = 10
+        noise, fbm = None, False
     else:
         c, sc = workloads.dambreak_2d()
         noise, fbm = None, False
@@ -386,7 +397,10 @@ def other_line(res, args, ws):
     desc = {"twophase3d": "3D two-phase VFSPH, two %s (rest density 1000 / 500) of %d particles each, "
                           "spacing 0.01, surface tension 0.07, volume-fraction update on" % (side, n3),
             "dambreak2d": "2D DFSPH dam break, 1.0 x 2.0 m block at 0.02 m (5,000 particles), 4 x 4 m box, "
-                          "dt 1e-3"}[res["kind"]]
+                          "dt 1e-3",
+            "dambreak3d_cs10": "3D DFSPH dam break, %d fluid + %d boundary particles, h=0.02, solver_cs 10 "
+                               "(dt<=1e-3, CFL), rho tol 0.1%%, div tol 1%%" % (res["fluid_particles"],
+                                                                              res["boundary_particles"])}[res["kind"]]
     return {"metric": METRIC, "value": res["fluid_particles"] * ws / (res["ms"] / 1e3), "unit": UNIT, "n_gpus": ws,
             "steps": res["steps"], "warmup": res["warmup"], "ms_per_step": res["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -400,7 +414,8 @@ def other_line(res, args, ws):
 def extra_workloads(dev, args):
     """The other configurations of the hot path at N = 1, for the headline line:
     the two-phase VFSPH pair (end of its 300-substep run), the 2D dam break
-    (substeps 4..1,000 of its run) and the adjoint's backward / forward ratio."""
+    (substeps 4..1,000 of its run), the headline dam break at solver_cs 10 (its
+    solves iterate) and the adjoint's backward / forward ratio."""
     out = {}
     tp = run_other("twophase3d", 20, 3, dev, develop=277)
     out["twophase3d"] = {"value": tp["fluid_particles"] / (tp["ms"] / 1e3), "unit": UNIT, "ms_per_step": tp["ms"],
@@ -417,6 +432,15 @@ def extra_workloads(dev, args):
                          **{k: other_line(d2, args, 1)["config"][k] for k in (
                              "fluid_particles", "boundary_particles", "mean_div_iter", "mean_incom_iter",
                              "max_density_error")}}
+    it = run_other("dambreak3d_cs10", 20, 3, dev, develop=77)
+    out["dambreak3d_cs10"] = {"value": it["fluid_particles"] / (it["ms"] / 1e3), "unit": UNIT, "ms_per_step": it["ms"],
+                              "window": "substeps %d..%d of a 100-substep run from rest (0.1 s of flow, the time the "
+                                        "headline's 500 substeps cover)" % (
+                                            it["develop"] + it["warmup"] + 1, it["develop"] + it["warmup"] + it["steps"]),
+                              "workload": other_line(it, args, 1)["config"]["workload"],
+                              **{k: other_line(it, args, 1)["config"][k] for k in (
+                                  "fluid_particles", "boundary_particles", "mean_div_iter", "mean_incom_iter",
+                                  "max_density_error")}}
     ad = run_adjoint(3, 1, dev)
     al = adjoint_line(ad, args, 1)
     out["adjoint"] = {"metric": "backward/forward time", "value": ad["ratio"], "unit": "ratio",
@@ -537,7 +561,7 @@ def main():
     ap.add_argument("--no-profile", action="store_true", help="skip the per-phase timing (roofline)")
     ap.add_argument("--tpp", type=int, default=0, help="threads per particle (0: autotune after warm-up)")
     ap.add_argument("--workload", default="dambreak3d",
-                    choices=["dambreak3d", "batched", "twophase3d", "dambreak2d", "adjoint"],
+                    choices=["dambreak3d", "batched", "twophase3d", "dambreak2d", "dambreak3d_cs10", "adjoint"],
                     help="dambreak3d: the headline line; the others print their own line")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched measurement added to the headline line (0: skip)")
@@ -569,7 +593,7 @@ def main():
         if dist:
             dist.destroy_process_group()
         return 0
-    if args.workload in ("twophase3d", "dambreak2d"):
+    if args.workload in ("twophase3d", "dambreak2d", "dambreak3d_cs10"):
         res = run_other(args.workload, args.steps, args.warmup, dev, develop=max(args.develop, 0),
                         n_side=args.n_side, hostloop=args.hostloop)
         if rank == 0:

@@ -55,7 +55,8 @@ def test_gpu_arm_line():
     assert d["batched"]["n_scenes"] == 4 and d["batched"]["value"] > 0
     # the window ends the 500-substep run; the other workloads ride on the same line
     assert d["config"]["window"].startswith("substeps 498..500 ")
-    for k in ("twophase3d", "dambreak2d"):
+    for k in ("twophase3d", "dambreak2d", "dambreak3d_cs10"):
         assert d[k]["value"] > 0 and d[k]["unit"] == "particle-steps/s" and d[k]["mean_incom_iter"] >= 2
     assert d["twophase3d"]["fluid_particles"] == 2000000 and d["dambreak2d"]["fluid_particles"] == 5000
+    assert d["dambreak3d_cs10"]["fluid_particles"] == 1000000
     assert d["adjoint"]["unit"] == "ratio" and 0 < d["adjoint"]["value"] < 3

@@ -88,8 +88,10 @@ __global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F) {
 // One pass: SPH_FBM_clean_tmp + pair loop of SPH_FBM_convect + SPH_FBM_diffuse +
 // SPH_FBM_check_tmp (sph.py:301-372).  The scene's last block evaluates its loop
 // test; the grid's last block sets the graph condition.
+// Up to two phases the pass is held to 48 registers (5 blocks per SM, measured
+// faster); with more phases the per-phase arrays would spill.
 template <int DIM, int P>
-__global__ void __launch_bounds__(kBlock) k_fbm_pass(KConst k, FluidBuf F, BoundBuf B,
+__global__ void __launch_bounds__(kBlock, P <= 2 ? 5 : 1) k_fbm_pass(KConst k, FluidBuf F, BoundBuf B,
                                                      cudaGraphConditionalHandle h, int use_cond) {
     __shared__ int any_neg;
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;

@@ -690,8 +690,10 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
 // reference's form with the range tests per candidate.  gs / vs scale the
 // gravity / viscosity terms by 1 or 0 (kernel-level calls may leave either
 // out; x * 1 is exact, so the full step's bits are unchanged).
+// One-scene instances are held to 48 registers (5 blocks per SM: measured
+// faster with surface tension, no spills); the batched ones would spill.
 template <int DIM, bool ST, int TPP, bool M>
-__global__ void __launch_bounds__(kBlock) k_advect(KConst k, FluidBuf F, BoundBuf B, float gs, float vs) {
+__global__ void __launch_bounds__(kBlock, M ? 1 : 5) k_advect(KConst k, FluidBuf F, BoundBuf B, float gs, float vs) {
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
     const int sc = f_block_scene<M>(k, first);
     const SceneConst &c = scene<M>(k, sc);
