@@ -195,7 +195,7 @@ struct FluidBuf {
     // fraction exceeds 0.99 (it takes part in surface tension), else kNoSurfTension
     float4 *normal;
     float4 *dens;      // W, sph_density, sph_compression, alpha_2: read together by the write-back
-    float4 *a1;
+    float4 *a1;        // alpha_1 (x, y, z), alpha
     float *vf, *vftmp;       // [P][cap]
     float4 *drift;           // [cap][P]: a particle's phases side by side (the pass gathers them together)
     float4 *facc;            // acce (fbm_acce)

@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
         U.sph_compression[pid] = dn.z;
         U.psi_adv[pid] = F.psiadv[s];
         if (F.wcp && U.pressure) U.pressure[pid] = F.wcp[s].x;
-        U.alpha[pid] = F.mpsi[s].w;
+        U.alpha[pid] = a1.w;  // alpha, stored beside alpha_1 by the density sweep
         U.alpha_2[pid] = dn.w;
         if (s - c.f_slot < st.f_in) {
             // slot in the reference's combined grid: cell offset over both sets, fluid first

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
         const float psi = k.vfsph ? comp_f : rho_f;
         const float psilo = k.vfsph ? __fsub_rn(comp_e, __fsub_rn(comp_f, comp)) : __fsub_rn(rho_e, __fsub_rn(rho_f, rho));
         F.dens[s] = make_float4(wsum, rho_f, comp_f, a2);
-        F.a1[s] = make_float4(a1x, a1y, a1z, 0.f);
+        F.a1[s] = make_float4(a1x, a1y, a1z, alpha);  // w: alpha again, for the write-back
         F.psilo[s] = psilo;
         F.mpsi[s] = make_float4(mp.x, psi, mp.z, alpha);
         // psi also rides in the current v_adv's unused w (the velocity sweeps carry
