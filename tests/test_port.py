@@ -58,3 +58,32 @@ def test_port_fp64_one_step(scene):
         scale = max(float(np.abs(b).max()), dens if f == "psi_adv" else 0.0)
         assert np.abs(a - b).max() <= 2e-7 * max(scale, 1e-30), (scene, f, np.abs(a - b).max(), scale)
     sim.close()
+
+
+@pytest.mark.parametrize("scene", ["dfsph3d", "vfsph3d"])
+def test_port_runs_are_bitwise_repeatable(scene):
+    """The C restatement fills each cell in id order and sums the compression
+    serially, so two runs give the same bits on any thread count (the long runs
+    compare the CUDA path against it over 1,000 substeps); its in-cell slots are
+    the id-ordered ranks of the reference's combined grid (fluid first)."""
+    init, _ = G.load(scene)
+    cfg = sph_config.load(*G.paths(scene))
+    fa, ba = G.init_arrays(init, "fluid"), G.init_arrays(init, "bound")
+    runs = []
+    for _ in range(2):
+        sim = PortSim(cfg, fa, ba, fbm=scene in G.FBM_SCENES)
+        stats = [sim.substep() for _ in range(8)]
+        runs.append((stats, {k: v.copy() for k, v in sim.fluid.a.items()}, {k: v.copy() for k, v in sim.bound.a.items()}))
+        sim.close()
+    (s0, f0, b0), (s1, f1, b1) = runs
+    assert s0 == s1
+    for a, b in ((f0, f1), (b0, b1)):
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    # in-cell slots: a cell's fluid particles in id order, then its boundary particles in id order
+    codes = np.concatenate([f0["neighb_cell_seq"], b0["neighb_cell_seq"]])
+    slots = np.concatenate([f0["neighb_in_cell_seq"], b0["neighb_in_cell_seq"]])
+    for code in np.unique(codes[codes > 0]):
+        idx = np.where(codes == code)[0]          # fluid ids first, each set in id order
+        s = slots[idx]
+        assert np.all(np.diff(s) == 1), (scene, code)
