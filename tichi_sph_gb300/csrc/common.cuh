@@ -444,6 +444,17 @@ __device__ __forceinline__ void visit_candidates_within(const int *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------------
+// Programmatic dependent launch.  The first statement of every kernel of the
+// step: wait until the kernel before it in the stream has completed and its
+// writes are visible, then let the kernel after it be scheduled.  Launched
+// with the programmatic attribute (TSPH_LAUNCH), a kernel's blocks are placed
+// on the SMs while its predecessor's last blocks still run, and start its work
+// the moment the predecessor has finished; launched plainly, both are no-ops.
+__device__ __forceinline__ void pdl_entry() {
+    asm volatile("griddepcontrol.wait;\n\tgriddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------------
 // Deterministic reductions in FP64 (warp shuffles, fixed trees).
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

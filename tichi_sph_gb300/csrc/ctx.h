@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "common.cuh"
 
 struct tsph_ctx {
@@ -42,6 +44,32 @@ struct tsph_ctx {
 };
 
 namespace tsph {
+
+// A kernel launch with programmatic stream serialisation: the kernel may be
+// scheduled before the one ahead of it in the stream has drained, and waits
+// for it in pdl_entry() (common.cuh), its first statement -- every kernel
+// launched this way has it.  Only outside a stream capture (host-driven loops,
+// the kernel-level entries): measured at 1M particles, stream launches gained
+// (grid 124 -> 114 us, velocity sweep 80 -> 75 us per launch) while the same
+// edges in the substep's CUDA graph made it slower (1.469 -> 1.487 ms), so
+// graphs get plain launches.
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args &&...args) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cap);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = cap == cudaStreamCaptureStatusNone ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+#define TSPH_LAUNCH(K, G, B, S, ...) ::tsph::launch_pdl(K, dim3(G), dim3(B), S, __VA_ARGS__)
 
 enum SolveKind { kSolveDiv = 0, kSolveDens = 1 };
 

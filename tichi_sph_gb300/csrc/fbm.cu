@@ -21,6 +21,7 @@
 namespace tsph {
 
 __global__ void k_fbm_begin(KConst k, cudaGraphConditionalHandle h, int use_cond) {
+    pdl_entry();
     __shared__ int any_sh;
     if (threadIdx.x == 0) any_sh = 0;
     __syncthreads();
@@ -45,6 +46,7 @@ __global__ void k_fbm_begin(KConst k, cudaGraphConditionalHandle h, int use_cond
 // First loop of SPH_FBM_convect, sph.py:331-345.
 template <int DIM, int P>
 __global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F) {
+    pdl_entry();
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int sc = k.f_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
     const SceneConst &c = k.sc[sc];
@@ -93,6 +95,7 @@ __global__ void __launch_bounds__(kBlock) k_fbm_drift(KConst k, FluidBuf F) {
 template <int DIM, int P>
 __global__ void __launch_bounds__(kBlock, P <= 2 ? 5 : 1) k_fbm_pass(KConst k, FluidBuf F, BoundBuf B,
                                                      cudaGraphConditionalHandle h, int use_cond) {
+    pdl_entry();
     __shared__ int any_neg;
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int sc = k.f_chunk_scene[(blockIdx.x * (int64_t)kBlock) / kChunk];
@@ -197,11 +200,11 @@ template <int P>
 static void fbm_pass_dim(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st, bool drift) {
     const int nb = blocks_for(c.F.cap);
     if (c.k.dim == 3) {
-        if (drift) k_fbm_drift<3, P><<<nb, kBlock, 0, st>>>(c.k, c.F);
-        else k_fbm_pass<3, P><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, h, use_cond);
+        if (drift) TSPH_LAUNCH((k_fbm_drift<3, P>), nb, kBlock, st, c.k, c.F);
+        else TSPH_LAUNCH((k_fbm_pass<3, P>), nb, kBlock, st, c.k, c.F, c.B, h, use_cond);
     } else {
-        if (drift) k_fbm_drift<2, P><<<nb, kBlock, 0, st>>>(c.k, c.F);
-        else k_fbm_pass<2, P><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, h, use_cond);
+        if (drift) TSPH_LAUNCH((k_fbm_drift<2, P>), nb, kBlock, st, c.k, c.F);
+        else TSPH_LAUNCH((k_fbm_pass<2, P>), nb, kBlock, st, c.k, c.F, c.B, h, use_cond);
     }
 }
 
@@ -222,7 +225,7 @@ void launch_fbm_begin(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, c
     cudaMemsetAsync(c.F.flagpass, 0, sizeof(int) * c.F.cap, st);
     c.launches += 2;
     fbm_dispatch(c, 0, 0, st, true);
-    k_fbm_begin<<<1, 256, 0, st>>>(c.k, h, use_cond);
+    TSPH_LAUNCH((k_fbm_begin), 1, 256, st, c.k, h, use_cond);
 }
 
 void launch_fbm_pass(tsph_ctx &c, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {

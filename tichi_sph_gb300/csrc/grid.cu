@@ -18,6 +18,7 @@ namespace tsph {
 // in v, so the minimum over particles is attained at max |v|.
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_cfl(KConst k, const float *__restrict__ vel, int64_t n) {
+    pdl_entry();
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * kBlock;
     // each warp keeps its running maximum for the scene it last saw and issues
@@ -79,6 +80,7 @@ __global__ void __launch_bounds__(kBlock) k_cfl(KConst k, const float *__restric
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_encode(KConst k, tsph_set U, int bound, int *__restrict__ count,
                                                    int *__restrict__ slot) {
+    pdl_entry();
     const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (i >= U.n) return;
     const int sc = bound ? k.b_user_scene[i] : k.f_user_scene[i];
@@ -150,6 +152,7 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total) {
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(ScanArgs a, int nblocks, unsigned int *tickets) {
+    pdl_entry();
     __shared__ int sh[33];
     const int g = blockIdx.y;
     const int64_t base = blockIdx.x * (int64_t)kScanTile + threadIdx.x * kScanItems;
@@ -188,6 +191,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(ScanArgs a, int nb
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_down(ScanArgs a, int nblocks, KConst k, unsigned int *ticket) {
+    pdl_entry();
     __shared__ int sh[33];
     const int g = blockIdx.y;
     const int64_t base = blockIdx.x * (int64_t)kScanTile + threadIdx.x * kScanItems;
@@ -226,6 +230,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(ScanArgs a, int nblo
 __global__ void __launch_bounds__(kBlock) k_scatter(KConst k, int bound, int64_t n, const int *__restrict__ code,
                                                     const int *__restrict__ slot, const int *__restrict__ start,
                                                     int *__restrict__ perm) {
+    pdl_entry();
     const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (i >= n) return;
     const int sc = bound ? k.b_user_scene[i] : k.f_user_scene[i];
@@ -269,6 +274,7 @@ __device__ __forceinline__ void slot_range(const SceneConst &c, long long shift,
 // sph_obj.py:65-73.
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_gather_fluid(KConst k, tsph_set U, FluidBuf F) {
+    pdl_entry();
     const int64_t u = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (u >= F.cap) return;
     const int sc = k.f_chunk_scene[u / kChunk];
@@ -294,6 +300,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fluid(KConst k, tsph_set U, F
 
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_gather_bound(KConst k, tsph_set U, BoundBuf B) {
+    pdl_entry();
     const int64_t u = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (u >= B.cap) return;
     const int sc = k.b_chunk_scene[u / kChunk];
@@ -344,6 +351,7 @@ template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, FluidBuf F,
                                                          const int *__restrict__ bstart, double *partials, int fbm,
                                                          int st_on) {
+    pdl_entry();
     __shared__ double sh[kBlock / 32];
     const int sc = k.f_ublock_scene[blockIdx.x];
     const SceneConst &c = k.sc[sc];
@@ -459,6 +467,7 @@ __global__ void __launch_bounds__(kBlock) k_update_fluid(KConst k, tsph_set U, F
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_update_bound(KConst k, tsph_set U, BoundBuf B,
                                                          const int *__restrict__ fstart) {
+    pdl_entry();
     const int64_t pid = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (pid >= U.n) return;
     const int sc = k.b_user_scene[pid];
@@ -497,6 +506,7 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_neighbor_stats(KConst k, int bound, FluidBuf F, BoundBuf B,
                                                            int32_t *counts, uint64_t *hash, int cand) {
+    pdl_entry();
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int64_t cap = bound ? B.cap : F.cap;
     if (s >= cap) return;
@@ -566,8 +576,8 @@ void launch_cfl(tsph_ctx &c, const tsph_set &f, cudaStream_t st) {
     if (nb < 1) nb = 1;
     if (nb > 4 * 152) nb = 4 * 152;
     c.launches += 1;
-    if (c.k.dim == 3) k_cfl<3><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n);
-    else k_cfl<2><<<nb, kBlock, 0, st>>>(c.k, f.vel, f.n);
+    if (c.k.dim == 3) TSPH_LAUNCH((k_cfl<3>), nb, kBlock, st, c.k, f.vel, f.n);
+    else TSPH_LAUNCH((k_cfl<2>), nb, kBlock, st, c.k, f.vel, f.n);
 }
 
 void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream_t st, bool with_cfl) {
@@ -580,13 +590,13 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     if (with_cfl) launch_cfl(c, f, sd);  // nothing before the first solve reads dt
     cudaMemsetAsync(c.B.count, 0, sizeof(int) * nn, sd);
     if (b.n > 0) {
-        if (c.k.dim == 3) k_encode<3><<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, b, 1, c.B.count, c.B.slot);
-        else k_encode<2><<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, b, 1, c.B.count, c.B.slot);
+        if (c.k.dim == 3) TSPH_LAUNCH((k_encode<3>), blocks_for(b.n), kBlock, sd, c.k, b, 1, c.B.count, c.B.slot);
+        else TSPH_LAUNCH((k_encode<2>), blocks_for(b.n), kBlock, sd, c.k, b, 1, c.B.count, c.B.slot);
     }
     cudaMemsetAsync(c.F.count, 0, sizeof(int) * nn, st);
     if (f.n > 0) {
-        if (c.k.dim == 3) k_encode<3><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, 0, c.F.count, c.F.slot);
-        else k_encode<2><<<blocks_for(f.n), kBlock, 0, st>>>(c.k, f, 0, c.F.count, c.F.slot);
+        if (c.k.dim == 3) TSPH_LAUNCH((k_encode<3>), blocks_for(f.n), kBlock, st, c.k, f, 0, c.F.count, c.F.slot);
+        else TSPH_LAUNCH((k_encode<2>), blocks_for(f.n), kBlock, st, c.k, f, 0, c.F.count, c.F.slot);
     }
     join_side(c, st);
     ScanArgs sa;
@@ -595,19 +605,19 @@ void launch_grid_build(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaSt
     sa.blocks[0] = c.S.scan_blocks; sa.blocks[1] = c.S.scan_blocks + c.S.scan_len / 2;
     sa.n = nn;
     const int nblk = (int)((nn + kScanTile - 1) / kScanTile);
-    k_scan_reduce<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk, c.k.dg->ticket + kGtScanF);
-    k_scan_down<<<dim3(nblk, 2), kScanThreads, 0, st>>>(sa, nblk, c.k, c.k.dg->ticket + kGtScanDone);
+    TSPH_LAUNCH((k_scan_reduce), dim3(nblk, 2), kScanThreads, st, sa, nblk, c.k.dg->ticket + kGtScanF);
+    TSPH_LAUNCH((k_scan_down), dim3(nblk, 2), kScanThreads, st, sa, nblk, c.k, c.k.dg->ticket + kGtScanDone);
     fork_side(c, st);
-    if (b.n > 0) k_scatter<<<blocks_for(b.n), kBlock, 0, sd>>>(c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm_u);
-    if (f.n > 0) k_scatter<<<blocks_for(f.n), kBlock, 0, st>>>(c.k, 0, f.n, f.neighb_cell_seq, c.F.slot, c.F.start, c.F.perm_u);
+    if (b.n > 0) TSPH_LAUNCH((k_scatter), blocks_for(b.n), kBlock, sd, c.k, 1, b.n, b.neighb_cell_seq, c.B.slot, c.B.start, c.B.perm_u);
+    if (f.n > 0) TSPH_LAUNCH((k_scatter), blocks_for(f.n), kBlock, st, c.k, 0, f.n, f.neighb_cell_seq, c.F.slot, c.F.start, c.F.perm_u);
     // each set's gather orders its cells by particle id as it copies (a
     // particle's slot is its rank among its cell's ids)
     if (c.k.dim == 3) {
-        k_gather_bound<3><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, b, c.B);
-        k_gather_fluid<3><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F);
+        TSPH_LAUNCH((k_gather_bound<3>), blocks_for(c.B.cap), kBlock, sd, c.k, b, c.B);
+        TSPH_LAUNCH((k_gather_fluid<3>), blocks_for(c.F.cap), kBlock, st, c.k, f, c.F);
     } else {
-        k_gather_bound<2><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, b, c.B);
-        k_gather_fluid<2><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, f, c.F);
+        TSPH_LAUNCH((k_gather_bound<2>), blocks_for(c.B.cap), kBlock, sd, c.k, b, c.B);
+        TSPH_LAUNCH((k_gather_fluid<2>), blocks_for(c.F.cap), kBlock, st, c.k, f, c.F);
     }
     join_side(c, st);
 }
@@ -621,11 +631,11 @@ void launch_unsort(tsph_ctx &c, const tsph_set &f, const tsph_set &b, cudaStream
     cudaStream_t sd = c.side ? c.side : st;
     fork_side(c, st);
     if (c.k.dim == 3) {
-        k_update_bound<3><<<nbb, kBlock, 0, sd>>>(c.k, b, c.B, c.F.start);
-        k_update_fluid<3><<<(int)c.k.f_ublocks, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
+        TSPH_LAUNCH((k_update_bound<3>), nbb, kBlock, sd, c.k, b, c.B, c.F.start);
+        TSPH_LAUNCH((k_update_fluid<3>), (int)c.k.f_ublocks, kBlock, st, c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
     } else {
-        k_update_bound<2><<<nbb, kBlock, 0, sd>>>(c.k, b, c.B, c.F.start);
-        k_update_fluid<2><<<(int)c.k.f_ublocks, kBlock, 0, st>>>(c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
+        TSPH_LAUNCH((k_update_bound<2>), nbb, kBlock, sd, c.k, b, c.B, c.F.start);
+        TSPH_LAUNCH((k_update_fluid<2>), (int)c.k.f_ublocks, kBlock, st, c.k, f, c.F, c.B.start, c.S.partials, fbm, st_on);
     }
     join_side(c, st);
 }

@@ -175,6 +175,7 @@ __device__ __forceinline__ void density_list_pair(const Geo &g, float4 pi, float
 // in the batched instance, whose scene lookups leave fewer registers, a loss.)
 template <int DIM, bool M>
 __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf F, BoundBuf B, double *partials) {
+    pdl_entry();
     __shared__ double sh[kBlock / 32];
     __shared__ unsigned int arrived;
     if (threadIdx.x == 0) arrived = 0;
@@ -340,6 +341,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_fluid(KConst k, FluidBuf 
 // SPH_prepare_alpha (sph.py:50-105 as called by main.py:190-197).
 template <int DIM, bool M>
 __global__ void __launch_bounds__(kBlock, 6) k_density_bound(KConst k, FluidBuf F, BoundBuf B) {
+    pdl_entry();
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int sc = b_block_scene<M>(k, blockIdx.x * (int64_t)kBlock);
     const SceneConst &c = scene<M>(k, sc);
@@ -416,6 +418,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_density_bound(KConst k, FluidBuf 
 // (sph.py:226); that is settled here without device work.  `flip` makes the
 // v_adv written by the advection sweep current.
 __global__ void k_solve_begin(KConst k, int kind, int flip, cudaGraphConditionalHandle h, int use_cond) {
+    pdl_entry();
     __shared__ int any_sh;
     if (threadIdx.x == 0) any_sh = 0;
     __syncthreads();
@@ -461,6 +464,7 @@ __global__ void k_solve_begin(KConst k, int kind, int flip, cudaGraphConditional
 // the sweep runs whatever the device-side loop condition says.
 template <int DIM, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBuf B, double *partials, int force) {
+    pdl_entry();
     __shared__ double sh[kBlock / 32];
     __shared__ unsigned int arrived;
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
@@ -543,6 +547,7 @@ __global__ void __launch_bounds__(kBlock, 6) k_psi(KConst k, FluidBuf F, BoundBu
 template <int DIM, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B, int kind,
                                                 cudaGraphConditionalHandle h, int use_cond, int force) {
+    pdl_entry();
     __shared__ unsigned int arrived;
     if (threadIdx.x == 0) arrived = 0;
     __syncthreads();
@@ -633,6 +638,7 @@ __global__ void __launch_bounds__(kBlock) k_vel(KConst k, FluidBuf F, BoundBuf B
 // First pass of SPH_advection_surface_tension_acc, sph.py:134-150: surface normals.
 template <int DIM, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBuf B) {
+    pdl_entry();
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
     const int sc = f_block_scene<M>(k, first);
     const SceneConst &c = scene<M>(k, sc);
@@ -694,6 +700,7 @@ __global__ void __launch_bounds__(kBlock) k_normal(KConst k, FluidBuf F, BoundBu
 // faster with surface tension, no spills); the batched ones would spill.
 template <int DIM, bool ST, int TPP, bool M>
 __global__ void __launch_bounds__(kBlock, M ? 1 : 5) k_advect(KConst k, FluidBuf F, BoundBuf B, float gs, float vs) {
+    pdl_entry();
     const int64_t first = blockIdx.x * (int64_t)(kBlock / TPP);
     const int sc = f_block_scene<M>(k, first);
     const SceneConst &c = scene<M>(k, sc);
@@ -842,11 +849,11 @@ void launch_density(tsph_ctx &c, cudaStream_t st) {
     fork_side(c, st);
     TSPH_M_DISPATCH(c.n_scenes > 1,
         if (c.k.dim == 3) {
-            k_density_bound<3, M><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, c.F, c.B);
-            k_density_fluid<3, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
+            TSPH_LAUNCH((k_density_bound<3, M>), blocks_for(c.B.cap), kBlock, sd, c.k, c.F, c.B);
+            TSPH_LAUNCH((k_density_fluid<3, M>), blocks_for(c.F.cap), kBlock, st, c.k, c.F, c.B, c.S.partials);
         } else {
-            k_density_bound<2, M><<<blocks_for(c.B.cap), kBlock, 0, sd>>>(c.k, c.F, c.B);
-            k_density_fluid<2, M><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials);
+            TSPH_LAUNCH((k_density_bound<2, M>), blocks_for(c.B.cap), kBlock, sd, c.k, c.F, c.B);
+            TSPH_LAUNCH((k_density_fluid<2, M>), blocks_for(c.F.cap), kBlock, st, c.k, c.F, c.B, c.S.partials);
         })
     join_side(c, st);
 }
@@ -854,18 +861,22 @@ void launch_density(tsph_ctx &c, cudaStream_t st) {
 // Measurement only: lets the next psi sweep run in full although the density
 // sweep did its first iteration's work.
 __global__ void k_clear_psi_ready(KConst k) {
+    pdl_entry();
     for (int s = threadIdx.x; s < k.n_scenes; s += blockDim.x) k.ss[s].psi_ready = 0;
 }
 
-void launch_clear_psi_ready(tsph_ctx &c, cudaStream_t st) { k_clear_psi_ready<<<1, 256, 0, st>>>(c.k); }
+void launch_clear_psi_ready(tsph_ctx &c, cudaStream_t st) { TSPH_LAUNCH((k_clear_psi_ready), 1, 256, st, c.k); }
 
-__global__ void k_status_or(KConst k, int bits) { atomicOr(&k.ss[0].status, bits); }
+__global__ void k_status_or(KConst k, int bits) {
+    pdl_entry();
+    atomicOr(&k.ss[0].status, bits);
+}
 
-void launch_status_or(tsph_ctx &c, int bits, cudaStream_t st) { k_status_or<<<1, 1, 0, st>>>(c.k, bits); }
+void launch_status_or(tsph_ctx &c, int bits, cudaStream_t st) { TSPH_LAUNCH((k_status_or), 1, 1, st, c.k, bits); }
 
 void launch_solve_begin(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
     c.launches += 1;
-    k_solve_begin<<<1, 256, 0, st>>>(c.k, kind, kind == kSolveDens ? 1 : 0, h, use_cond);
+    TSPH_LAUNCH((k_solve_begin), 1, 256, st, c.k, kind, kind == kSolveDens ? 1 : 0, h, use_cond);
 }
 
 // Threads per particle of the list sweeps (1, 2, 4 or 8); see Lanes.
@@ -884,8 +895,8 @@ void launch_psi(tsph_ctx &c, cudaStream_t st, int force) {
     const int tpp = c.tpp;
     const int nb = tpp_blocks(c.F.cap, tpp);
     TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
-        if (c.k.dim == 3) k_psi<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials, force);
-        else k_psi<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, c.S.partials, force)))
+        if (c.k.dim == 3) TSPH_LAUNCH((k_psi<3, TPP, M>), nb, kBlock, st, c.k, c.F, c.B, c.S.partials, force);
+        else TSPH_LAUNCH((k_psi<2, TPP, M>), nb, kBlock, st, c.k, c.F, c.B, c.S.partials, force)))
 }
 
 void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st, int force) {
@@ -893,8 +904,8 @@ void launch_vel(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_con
     const int tpp = c.tpp;
     const int nb = tpp_blocks(c.F.cap, tpp);
     TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
-        if (c.k.dim == 3) k_vel<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond, force);
-        else k_vel<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, kind, h, use_cond, force)))
+        if (c.k.dim == 3) TSPH_LAUNCH((k_vel<3, TPP, M>), nb, kBlock, st, c.k, c.F, c.B, kind, h, use_cond, force);
+        else TSPH_LAUNCH((k_vel<2, TPP, M>), nb, kBlock, st, c.k, c.F, c.B, kind, h, use_cond, force)))
 }
 
 void launch_solve_iter(tsph_ctx &c, int kind, cudaGraphConditionalHandle h, int use_cond, cudaStream_t st) {
@@ -911,17 +922,17 @@ void launch_advect(tsph_ctx &c, cudaStream_t st, int terms) {
     TSPH_M_DISPATCH(c.n_scenes > 1, TSPH_TPP_DISPATCH(tpp,
         if (c.k.dim == 3) {
             if (st_on) {
-                k_normal<3, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
-                k_advect<3, true, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, gs, vs);
+                TSPH_LAUNCH((k_normal<3, TPP, M>), nb, kBlock, st, c.k, c.F, c.B);
+                TSPH_LAUNCH((k_advect<3, true, TPP, M>), nb, kBlock, st, c.k, c.F, c.B, gs, vs);
             } else {
-                k_advect<3, false, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, gs, vs);
+                TSPH_LAUNCH((k_advect<3, false, TPP, M>), nb, kBlock, st, c.k, c.F, c.B, gs, vs);
             }
         } else {
             if (st_on) {
-                k_normal<2, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B);
-                k_advect<2, true, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, gs, vs);
+                TSPH_LAUNCH((k_normal<2, TPP, M>), nb, kBlock, st, c.k, c.F, c.B);
+                TSPH_LAUNCH((k_advect<2, true, TPP, M>), nb, kBlock, st, c.k, c.F, c.B, gs, vs);
             } else {
-                k_advect<2, false, TPP, M><<<nb, kBlock, 0, st>>>(c.k, c.F, c.B, gs, vs);
+                TSPH_LAUNCH((k_advect<2, false, TPP, M>), nb, kBlock, st, c.k, c.F, c.B, gs, vs);
             }
         }))
 }

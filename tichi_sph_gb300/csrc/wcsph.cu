@@ -29,6 +29,7 @@ __device__ __forceinline__ float pow7(float r) {
 
 template <bool M>
 __global__ void __launch_bounds__(kBlock) k_wc_pressure(KConst k, FluidBuf F, BoundBuf B, const float *bpress) {
+    pdl_entry();
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     if (s < F.cap) {
         const SceneConst &c = scene<M>(k, f_block_scene<M>(k, s - (s % kChunk)));
@@ -51,6 +52,7 @@ __global__ void __launch_bounds__(kBlock) k_wc_pressure(KConst k, FluidBuf F, Bo
 
 template <int DIM, bool M>
 __global__ void __launch_bounds__(kBlock) k_wc_acce(KConst k, FluidBuf F, BoundBuf B) {
+    pdl_entry();
     const int64_t s = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int sc = f_block_scene<M>(k, blockIdx.x * (int64_t)kBlock);
     const SceneConst &c = scene<M>(k, sc);
@@ -88,6 +90,7 @@ template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_map_velocity(KConst k, FluidBuf F, tsph_set U, float lb0, float lb1,
                                                          float lb2, float dist, int n0, int n1, int n2,
                                                          float *out) {
+    pdl_entry();
     const int64_t I = blockIdx.x * (int64_t)kBlock + threadIdx.x;
     const int64_t total = (int64_t)n0 * n1 * (DIM == 3 ? n2 : 1);
     if (I >= total) return;
@@ -136,13 +139,13 @@ void launch_wc(tsph_ctx &c, const tsph_set &b, cudaStream_t st) {
     const int64_t n = c.F.cap > c.B.cap ? c.F.cap : c.B.cap;
     c.launches += 2;
     if (c.n_scenes > 1) {
-        k_wc_pressure<true><<<blocks_for(n), kBlock, 0, st>>>(c.k, c.F, c.B, b.pressure);
-        if (c.k.dim == 3) k_wc_acce<3, true><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
-        else k_wc_acce<2, true><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+        TSPH_LAUNCH((k_wc_pressure<true>), blocks_for(n), kBlock, st, c.k, c.F, c.B, b.pressure);
+        if (c.k.dim == 3) TSPH_LAUNCH((k_wc_acce<3, true>), blocks_for(c.F.cap), kBlock, st, c.k, c.F, c.B);
+        else TSPH_LAUNCH((k_wc_acce<2, true>), blocks_for(c.F.cap), kBlock, st, c.k, c.F, c.B);
     } else {
-        k_wc_pressure<false><<<blocks_for(n), kBlock, 0, st>>>(c.k, c.F, c.B, b.pressure);
-        if (c.k.dim == 3) k_wc_acce<3, false><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
-        else k_wc_acce<2, false><<<blocks_for(c.F.cap), kBlock, 0, st>>>(c.k, c.F, c.B);
+        TSPH_LAUNCH((k_wc_pressure<false>), blocks_for(n), kBlock, st, c.k, c.F, c.B, b.pressure);
+        if (c.k.dim == 3) TSPH_LAUNCH((k_wc_acce<3, false>), blocks_for(c.F.cap), kBlock, st, c.k, c.F, c.B);
+        else TSPH_LAUNCH((k_wc_acce<2, false>), blocks_for(c.F.cap), kBlock, st, c.k, c.F, c.B);
     }
 }
 
