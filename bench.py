@@ -524,7 +524,8 @@ def run_reference(args, rank, ws):
         "config": {"workload": "3D DFSPH dam break, %d fluid + %d boundary particles, h=%g, dt<=%g (CFL), "
                                "rho tol 0.1%%, div tol 1%%" % (nf, res["n_bound"], 2 * args.spacing, args.spacing / 50),
                    "window": "substeps 1..%d of the run from rest (a bounded CPU sample; the GPU arm times the "
-                             "end of the 500-substep run, where the solves iterate more)" % len(res["iters"]),
+                             "end of the 500-substep run, the developed flow; both at the solvers' floor of two "
+                             "iterations each)" % len(res["iters"]),
                    "fluid_particles": nf},
         "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
