@@ -243,11 +243,13 @@ def cpu_baseline(n_side, budget_s, max_steps, spacing=0.01):
             "ms_per_step": el / steps * 1e3, "iters": iters, "n_bound": sim.bound.part_num[None]}
 
 
-def run_batched(n_scenes, steps, warmup, dev, dist=None, rank=0, ws=1):
+def run_batched(n_scenes, steps, warmup, dev, dist=None, rank=0, ws=1, hostloop=False):
     """Scenes of workloads.batched_dambreaks stepped (a) as one batch and (b) one at
     a time, each through its own plain context: particle-steps/s of both.  With
     several ranks the scenes are split by partition_scenes (no collective while
-    stepping); times are the maximum over ranks, particle counts the totals."""
+    stepping); times are the maximum over ranks, particle counts the totals.
+    ``hostloop``: the batch launches every kernel on its own (as profilers list
+    them) instead of one CUDA graph per substep."""
     import torch
     from tichi_sph_gb300 import sph_config, workloads, Solver
     from tichi_sph_gb300.batch import BatchSolver, gather_scenes
@@ -264,7 +266,7 @@ def run_batched(n_scenes, steps, warmup, dev, dist=None, rank=0, ws=1):
         sim.init_scenario()
         sims.append(sim)
     fluid, bound, nf, nb = gather_scenes(sims, device=dev)
-    batch = BatchSolver([s.config for s in sims], fluid, bound, nf, nb)
+    batch = BatchSolver([s.config for s in sims], fluid, bound, nf, nb, use_graph=not hostloop)
     stream = torch.cuda.current_stream(dev)
     for _ in range(warmup):
         batch.substep()
@@ -581,7 +583,7 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     if args.workload == "batched":
-        res = run_batched(256, args.steps, args.warmup, dev, dist, rank, ws)
+        res = run_batched(256, args.steps, args.warmup, dev, dist, rank, ws, hostloop=args.hostloop)
         if rank == 0:
             print(json.dumps(batched_line(res, args, ws)), flush=True)
         if dist:
